@@ -1,0 +1,712 @@
+// decaes_gpu.cu -- kernels and host orchestration of libdecaes_gpu.so.
+//
+// Call flow of decaes_t2map_t2part (host buffers):
+//   H2D image -> [resident angle-ensemble basis, cached per parameter key]
+//   -> NaN-fill outputs -> threshold compaction -> persistent warp-per-voxel
+//   solve (flip-angle search, EPG basis, regularized NNLS, save_results! and
+//   fused T2part) -> optional FP32 narrowing -> D2H outputs.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "decaes_gpu.h"
+#include "epg.cuh"
+#include "host.h"
+#include "t2map_device.cuh"
+
+namespace dk {
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+
+// Angle-ensemble basis As[m,n,K] and dAs/dalpha (EPGBasisSetEnsemble +
+// ∇epg_decay_basis!, src/T2mapSEcorr.jl:322-371): one curve per thread, the
+// value part of a forward-mode dual evaluation.
+__global__ void k_ensemble(int m, int n, int K, double TE, double T1, int beta180, double beta, const double *t2,
+                           const double *angles, double *As, double *dAs, dx::Dual *work) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * K) return;
+    int j = t % n, k = t / n;
+    dx::Dual *S = work + (long)t * 3 * m;                    // 3m recursion states
+    dx::Dual *out = work + (long)n * K * 3 * m + (long)t * m;  // m curve values
+    double *Av = As + ((long)k * n + j) * m, *dAv = dAs + ((long)k * n + j) * m;
+    if (beta180) {
+        dx::FlatCoef<dx::Dual> q = dx::flat_coef_dual(angles[k], TE, t2[j], T1);
+        dx::epg_flat_inplace(m, q, S, 1, out, 1);
+    } else {
+        dx::VecCoef<dx::Dual> q = dx::vec_coef_dual(angles[k], TE, t2[j], T1, beta);
+        dx::epg_vec_inplace(m, q, S, 1, out, 1);
+    }
+    for (int i = 0; i < m; ++i) { Av[i] = out[i].v; dAv[i] = out[i].d; }
+}
+
+// Single basis at a fixed angle (SetFlipAngle), one curve per thread.
+__global__ void k_basis_fixed(int m, int n, double alpha, double TE, double T1, int beta180, double beta,
+                              const double *t2, double *A, double *work) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    double *S = work + (long)j * 3 * m;
+    if (beta180) {
+        dx::FlatCoef<double> q = dx::flat_coef(alpha, TE, t2[j], T1);
+        dx::epg_flat_inplace(m, q, S, 1, A + (long)j * m, 1);
+    } else {
+        dx::VecCoef<double> q = dx::vec_coef(alpha, TE, t2[j], T1, beta);
+        dx::epg_vec_inplace(m, q, S, 1, A + (long)j * m, 1);
+    }
+}
+
+__global__ void k_fill(double *p, long len, double v) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < len; i += (long)gridDim.x * blockDim.x) p[i] = v;
+}
+
+// indices = filter(I -> image[I, 1] > Threshold, CartesianIndices(MatrixSize)),
+// src/T2mapSEcorr.jl:177 (order of the compacted list does not matter:
+// voxels are independent).
+__global__ void k_compact(const void *image, int f32, long V, double thr, int *vidx, int *nvox) {
+    for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < V; v += (long)gridDim.x * blockDim.x) {
+        double b = f32 ? (double)static_cast<const float *>(image)[v] : static_cast<const double *>(image)[v];
+        bool keep = b > thr;
+        unsigned msk = __ballot_sync(__activemask(), keep);
+        if (keep) {
+            int leader = __ffs(msk) - 1, lane = threadIdx.x & 31, base = 0;
+            if (lane == leader) base = atomicAdd(nvox, __popc(msk));
+            base = __shfl_sync(msk, base, leader);
+            vidx[base + __popc(msk & ((1u << lane) - 1))] = (int)v;
+        }
+    }
+}
+
+// Persistent voxel solver: one warp per voxel, voxels pulled from a counter.
+__global__ void __launch_bounds__(32) k_voxels(Params P) {
+    extern __shared__ double smem[];
+    Warp w;
+    w.P = &P;
+    w.lane = threadIdx.x & 31;
+    w.nnls_caps = 0;
+    w.loop_caps = 0;
+    const int n = P.n, lda = P.lda;
+    double *p = smem;
+    w.s.C = p; p += (long)lda * n;
+    w.s.b = p; p += lda;
+    w.s.zz = p; p += lda;
+    w.data = p; p += lda;
+    w.s.x = p; p += n;
+    w.s.w = p; p += n;
+    w.xout = p; p += n;
+    p += 8;
+    w.s.idx = reinterpret_cast<int *>(p);
+    w.s.diag = reinterpret_cast<unsigned char *>(w.s.idx + 2 * n);
+    w.s.lda = lda;
+    w.scr = P.scratch + (long)blockIdx.x * P.scr_stride;
+    const int nvox = *P.nvox;
+    for (;;) {
+        int t = 0;
+        if (w.lane == 0) t = atomicAdd(P.counter, 1);
+        t = __shfl_sync(FULL, t, 0);
+        if (t >= nvox) break;
+        process_voxel(w, (long)P.vidx[t]);
+    }
+    if (w.lane == 0) {
+        if (w.nnls_caps) atomicAdd(&P.stats[0], (unsigned long long)w.nnls_caps);
+        if (w.loop_caps) atomicAdd(&P.stats[1], (unsigned long long)w.loop_caps);
+    }
+}
+
+// Standalone T2partSEcorr (src/T2partSEcorr.jl:95-138): one thread per voxel.
+template <class T>
+__global__ void k_t2part(const T *dist, long V, int n, int sp0, int sp1, int mp0, int mp1, const double *logt2,
+                         const double *weights, double *sfr, double *sgm, double *mfr, double *mgm) {
+    for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < V; v += (long)gridDim.x * blockDim.x) {
+        bool anynan = false;
+        for (int j = 0; j < n; ++j) anynan |= isnan((double)dist[v + V * j]);
+        if (anynan) continue;
+        double sd = 0, ssp = 0, smp = 0, dsp = 0, dmp = 0;
+        for (int j = 0; j < n; ++j) sd = __dadd_rn(sd, (double)dist[v + V * j]);
+        for (int j = sp0; j <= sp1; ++j) {
+            double d = dist[v + V * j];
+            dsp = __dadd_rn(dsp, __dmul_rn(d, logt2[j]));
+            ssp = __dadd_rn(ssp, d);
+        }
+        for (int j = mp0; j <= mp1; ++j) {
+            double d = dist[v + V * j];
+            dmp = __dadd_rn(dmp, __dmul_rn(d, logt2[j]));
+            smp = __dadd_rn(smp, d);
+        }
+        if (sd > 0) {
+            if (weights) {
+                double dw = 0;
+                for (int j = 0; j < n; ++j) dw = __dadd_rn(dw, __dmul_rn((double)dist[v + V * j], weights[j]));
+                sfr[v] = dw / sd;
+            } else {
+                sfr[v] = ssp / sd;
+            }
+            mfr[v] = smp / sd;
+        }
+        if (ssp > 0) sgm[v] = exp(dsp / ssp);
+        if (smp > 0) mgm[v] = exp(dmp / smp);
+    }
+}
+
+__global__ void k_narrow(const double *src, float *dst, long len) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < len; i += (long)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
+}
+
+}  // namespace dk
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+struct BasisKey {
+    int m, n, K, beta180;
+    double TE, T1, t2lo, t2hi, minang, beta, fixed;
+    bool operator<(const BasisKey &o) const {
+        return std::tie(m, n, K, beta180, TE, T1, t2lo, t2hi, minang, beta, fixed) <
+               std::tie(o.m, o.n, o.K, o.beta180, o.TE, o.T1, o.t2lo, o.t2hi, o.minang, o.beta, o.fixed);
+    }
+};
+struct Basis {
+    double *t2 = nullptr, *logt2 = nullptr, *angles = nullptr, *As = nullptr, *dAs = nullptr, *fixed = nullptr;
+    std::vector<double> h_t2, h_angles;
+    size_t bytes = 0;
+    long last_use = 0;
+};
+
+}  // namespace
+
+struct decaes_ctx {
+    int device = 0;
+    size_t budget = 0, used = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8];
+    std::string err;
+    decaes_stats stats{};
+    std::map<std::string, DevBuf> bufs;
+    std::map<BasisKey, Basis> bases;
+    long tick = 0;
+    int sms = 0;
+    size_t smem_optin = 0;
+    std::mutex mu;
+};
+
+namespace {
+
+int fail(decaes_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+#define CK(call)                                                                             \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) return fail(ctx, DECAES_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Grow-only named device buffers, accounted against the HBM budget.
+int buf(decaes_ctx *ctx, const std::string &name, size_t bytes, void **out) {
+    DevBuf &b = ctx->bufs[name];
+    if (b.bytes < bytes) {
+        if (b.p) { cudaFree(b.p); ctx->used -= b.bytes; b.p = nullptr; b.bytes = 0; }
+        if (ctx->used + bytes > ctx->budget)
+            return fail(ctx, DECAES_ENOMEM, "device allocation of " + std::to_string(bytes) + " bytes for '" + name +
+                                                "' exceeds the context's HBM budget");
+        cudaError_t e = cudaMalloc(&b.p, bytes);
+        if (e != cudaSuccess) return fail(ctx, DECAES_ECUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        b.bytes = bytes;
+        ctx->used += bytes;
+    }
+    *out = b.p;
+    return DECAES_OK;
+}
+
+size_t esize(int dtype) { return dtype == DECAES_F32 ? 4 : 8; }
+
+// Resident per-parameter basis: T2 grid, angle grid, As and dAs (or the fixed basis).
+int get_basis(decaes_ctx *ctx, const decaes_t2map_opts &o, Basis **out) {
+    const bool fixed = !std::isnan(o.SetFlipAngle);
+    BasisKey key{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.RefConAngle == 180.0, o.TE, o.T1, o.T2Range[0], o.T2Range[1],
+                 fixed ? 0.0 : o.MinRefAngle, o.RefConAngle, fixed ? o.SetFlipAngle : -1.0};
+    auto it = ctx->bases.find(key);
+    if (it != ctx->bases.end()) {
+        it->second.last_use = ++ctx->tick;
+        *out = &it->second;
+        return DECAES_OK;
+    }
+    if (ctx->bases.size() >= 8) {  // evict the least recently used key
+        auto lru = ctx->bases.begin();
+        for (auto i = ctx->bases.begin(); i != ctx->bases.end(); ++i)
+            if (i->second.last_use < lru->second.last_use) lru = i;
+        Basis &b = lru->second;
+        cudaFree(b.t2); cudaFree(b.logt2); cudaFree(b.angles); cudaFree(b.As); cudaFree(b.dAs); cudaFree(b.fixed);
+        ctx->used -= b.bytes;
+        ctx->bases.erase(lru);
+    }
+    const int m = o.nTE, n = o.nT2, K = key.K;
+    Basis b;
+    b.h_t2 = dh::julia_logrange(o.T2Range[0], o.T2Range[1], n);
+    std::vector<double> logt2(n);
+    for (int j = 0; j < n; ++j) logt2[j] = std::log(b.h_t2[j]);
+    b.h_angles = fixed ? std::vector<double>{o.SetFlipAngle} : dh::julia_range(o.MinRefAngle, 180.0, K);
+    size_t mnk = (size_t)m * n * K;
+    b.bytes = sizeof(double) * (2 * n + K + (fixed ? (size_t)m * n : 2 * mnk));
+    if (ctx->used + b.bytes > ctx->budget) return fail(ctx, DECAES_ENOMEM, "resident basis exceeds the HBM budget");
+    CK(cudaMalloc(&b.t2, sizeof(double) * n));
+    CK(cudaMalloc(&b.logt2, sizeof(double) * n));
+    CK(cudaMalloc(&b.angles, sizeof(double) * K));
+    CK(cudaMemcpyAsync(b.t2, b.h_t2.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(b.logt2, logt2.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(b.angles, b.h_angles.data(), sizeof(double) * K, cudaMemcpyHostToDevice, ctx->stream));
+    const int beta180 = o.RefConAngle == 180.0;
+    if (fixed) {
+        CK(cudaMalloc(&b.fixed, sizeof(double) * m * n));
+        void *work;
+        if (int rc = buf(ctx, "epgwork", sizeof(double) * 3 * (size_t)m * n, &work)) return rc;
+        dk::k_basis_fixed<<<(n + 63) / 64, 64, 0, ctx->stream>>>(m, n, o.SetFlipAngle, o.TE, o.T1, beta180, o.RefConAngle,
+                                                                 b.t2, b.fixed, (double *)work);
+    } else {
+        CK(cudaMalloc(&b.As, sizeof(double) * mnk));
+        CK(cudaMalloc(&b.dAs, sizeof(double) * mnk));
+        void *work;
+        if (int rc = buf(ctx, "epgwork", sizeof(dx::Dual) * 4 * (size_t)m * n * K, &work)) return rc;
+        dk::k_ensemble<<<(n * K + 63) / 64, 64, 0, ctx->stream>>>(m, n, K, o.TE, o.T1, beta180, o.RefConAngle, b.t2,
+                                                                  b.angles, b.As, b.dAs, (dx::Dual *)work);
+    }
+    CK(cudaGetLastError());
+    ctx->used += b.bytes;
+    b.last_use = ++ctx->tick;
+    auto res = ctx->bases.emplace(key, b);
+    *out = &res.first->second;
+    return DECAES_OK;
+}
+
+struct OutMap {  // device double buffers for each output
+    double *dist, *gdn, *ggm, *gva, *fnr, *snr, *alpha, *resnorm, *decaycurve, *mu, *chi2f, *basis;
+    double *sfr, *sgm, *mfr, *mgm;
+    size_t total;
+};
+
+// Core: everything on device pointers; host-buffer entry points wrap it with copies.
+int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_opts *po, const void *d_image,
+              int dtype, const void *d_b1, OutMap &out, cudaStream_t st, int *launches) {
+    const int m = o.nTE, n = o.nT2;
+    const long V = (long)o.MatrixSize[0] * o.MatrixSize[1] * o.MatrixSize[2];
+    if (m > 128) return fail(ctx, DECAES_EINVAL, "nTE > 128 is not supported by this build");
+    if (n > 256) return fail(ctx, DECAES_EINVAL, "nT2 > 256 is not supported by this build");
+    const bool fixed = !std::isnan(o.SetFlipAngle);
+    if (!fixed && o.nRefAngles > 256) return fail(ctx, DECAES_EINVAL, "nRefAngles > 256 is not supported by this build");
+    Basis *B;
+    if (int rc = get_basis(ctx, o, &B)) return rc;
+    int nl = 0;
+    // T2part plan (fused)
+    dh::T2partPlan pp{};
+    double *d_weights = nullptr;
+    if (po) {
+        std::string e = dh::t2part_plan(*po, pp);
+        if (!e.empty()) return fail(ctx, DECAES_EINVAL, e);
+        if (!pp.weights.empty()) {
+            void *w;
+            if (int rc = buf(ctx, "weights", sizeof(double) * n, &w)) return rc;
+            d_weights = (double *)w;
+            CK(cudaMemcpyAsync(d_weights, pp.weights.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        }
+    }
+    // NaN-fill outputs
+    {
+        int g = std::min<long>(4L * ctx->sms * 8, (long)(out.total + 255) / 256);
+        dk::k_fill<<<std::max(g, 1), 256, 0, st>>>(out.dist, (long)out.total, NAN);
+        ++nl;
+    }
+    // compaction
+    void *vidx, *cnt;
+    if (int rc = buf(ctx, "vidx", sizeof(int) * (size_t)std::max<long>(V, 1), &vidx)) return rc;
+    if (int rc = buf(ctx, "counters", 64, &cnt)) return rc;
+    CK(cudaMemsetAsync(cnt, 0, 64, st));
+    int *d_nvox = (int *)cnt, *d_counter = (int *)cnt + 1;
+    unsigned long long *d_stats = (unsigned long long *)((char *)cnt + 16);
+    {
+        int g = (int)std::min<long>(8L * ctx->sms, (V + 255) / 256);
+        dk::k_compact<<<std::max(g, 1), 256, 0, st>>>(d_image, dtype == DECAES_F32, V, o.Threshold, (int *)vidx, d_nvox);
+        ++nl;
+    }
+    // persistent voxel kernel
+    dk::Params P{};
+    P.m = m; P.n = n; P.K = fixed ? 1 : o.nRefAngles; P.M = m + n; P.lda = (m + n) | 1;
+    P.reg = o.Reg; P.chi2factor = o.Chi2Factor; P.noiselevel = o.NoiseLevel;
+    P.mineval = o.nRefAnglesMin; P.maxeval = o.nRefAngles;
+    P.angle_mode = d_b1 ? 2 : (fixed ? 1 : 0);
+    P.fixed_angle = o.SetFlipAngle;
+    P.beta180 = o.RefConAngle == 180.0; P.beta = o.RefConAngle; P.TE = o.TE; P.T1 = o.T1;
+    P.V = V; P.nvox = d_nvox; P.vidx = (const int *)vidx;
+    P.image = d_image; P.image_f32 = dtype == DECAES_F32; P.b1map = d_b1;
+    P.t2 = B->t2; P.logt2 = B->logt2; P.angles = B->angles; P.As = B->As; P.dAs = B->dAs; P.basis_fixed = B->fixed;
+    P.counter = d_counter; P.stats = d_stats;
+    P.dist = out.dist; P.gdn = out.gdn; P.ggm = out.ggm; P.gva = out.gva; P.fnr = out.fnr; P.snr = out.snr;
+    P.alpha = out.alpha; P.resnorm = out.resnorm; P.decaycurve = out.decaycurve; P.mu = out.mu; P.chi2f = out.chi2f;
+    P.basis_out = out.basis;
+    P.need_chi2 = o.SaveRegParam ? 1 : 0;
+    if (po) {
+        P.fuse_t2part = 1; P.sp0 = pp.sp0; P.sp1 = pp.sp1; P.mp0 = pp.mp0; P.mp1 = pp.mp1; P.weights = d_weights;
+        P.sfr = out.sfr; P.sgm = out.sgm; P.mfr = out.mfr; P.mgm = out.mgm;
+    }
+    long wsm = dk::warp_smem_doubles(m, n, P.lda);
+    size_t smem = (size_t)wsm * sizeof(double);
+    if (smem > ctx->smem_optin)
+        return fail(ctx, DECAES_EINVAL, "nTE/nT2 too large: the per-voxel workspace (" + std::to_string(smem) +
+                                            " bytes) exceeds shared memory per block");
+    P.epg_lanes = (int)std::min<long>(32, ((long)P.lda * n) / (3L * m));
+    CK(cudaFuncSetAttribute(dk::k_voxels, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dk::k_voxels, 32, smem));
+    if (per_sm < 1) return fail(ctx, DECAES_EINVAL, "voxel kernel cannot be resident with this workspace size");
+    const int grid = per_sm * ctx->sms;
+    P.scr_stride = dk::warp_scratch_doubles(m, n, P.K);
+    void *scr;
+    if (int rc = buf(ctx, "scratch", sizeof(double) * (size_t)P.scr_stride * grid, &scr)) return rc;
+    P.scratch = (double *)scr;
+    cudaEventRecord(ctx->ev[2], st);
+    dk::k_voxels<<<grid, 32, smem, st>>>(P);
+    cudaEventRecord(ctx->ev[3], st);
+    ++nl;
+    CK(cudaGetLastError());
+    *launches += nl;
+    return DECAES_OK;
+}
+
+int out_layout(decaes_ctx *ctx, const decaes_t2map_opts &o, bool want_t2part, OutMap &om) {
+    const long V = (long)o.MatrixSize[0] * o.MatrixSize[1] * o.MatrixSize[2];
+    const bool fixed = !std::isnan(o.SetFlipAngle);
+    size_t tot = 0;
+    auto take = [&](size_t len) { size_t off = tot; tot += len; return off; };
+    size_t o_dist = take((size_t)V * o.nT2), o_maps = take((size_t)V * 6);
+    size_t o_res = o.SaveResidualNorm ? take(V) : SIZE_MAX;
+    size_t o_dc = o.SaveDecayCurve ? take((size_t)V * o.nTE) : SIZE_MAX;
+    size_t o_mu = o.SaveRegParam ? take(V) : SIZE_MAX, o_chi = o.SaveRegParam ? take(V) : SIZE_MAX;
+    size_t o_basis = (o.SaveNNLSBasis && !fixed) ? take((size_t)V * o.nTE * o.nT2) : SIZE_MAX;
+    size_t o_part = want_t2part ? take((size_t)V * 4) : SIZE_MAX;
+    void *p;
+    if (int rc = buf(ctx, "outputs", sizeof(double) * tot, &p)) return rc;
+    double *d = (double *)p;
+    auto at = [&](size_t off) { return off == SIZE_MAX ? nullptr : d + off; };
+    om.dist = at(o_dist);
+    om.gdn = d + o_maps; om.ggm = om.gdn + V; om.gva = om.ggm + V; om.fnr = om.gva + V; om.snr = om.fnr + V; om.alpha = om.snr + V;
+    om.resnorm = at(o_res); om.decaycurve = at(o_dc); om.mu = at(o_mu); om.chi2f = at(o_chi); om.basis = at(o_basis);
+    double *pt = at(o_part);
+    om.sfr = pt; om.sgm = pt ? pt + V : nullptr; om.mfr = pt ? pt + 2 * V : nullptr; om.mgm = pt ? pt + 3 * V : nullptr;
+    om.total = tot;
+    return DECAES_OK;
+}
+
+// Copy one device double output to a caller host buffer of the call dtype.
+int copy_out(decaes_ctx *ctx, const double *src, void *dst, size_t len, int dtype, cudaStream_t st, int *launches) {
+    if (!dst || !src || !len) return DECAES_OK;
+    if (dtype == DECAES_F64) {
+        CK(cudaMemcpyAsync(dst, src, sizeof(double) * len, cudaMemcpyDeviceToHost, st));
+    } else {
+        void *tmp;
+        if (int rc = buf(ctx, "narrow", sizeof(float) * len, &tmp)) return rc;
+        int g = (int)std::min<long>(8L * ctx->sms, ((long)len + 255) / 256);
+        dk::k_narrow<<<std::max(g, 1), 256, 0, st>>>(src, (float *)tmp, (long)len);
+        ++*launches;
+        CK(cudaMemcpyAsync(dst, tmp, sizeof(float) * len, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));  // `narrow` is reused by the next output
+    }
+    return DECAES_OK;
+}
+
+int check_both(decaes_ctx *ctx, const decaes_t2map_opts *mo, const decaes_t2part_opts *po, int dtype) {
+    if (!ctx) return DECAES_EINVAL;
+    if (dtype != DECAES_F32 && dtype != DECAES_F64) return fail(ctx, DECAES_EINVAL, "dtype must be DECAES_F32 or DECAES_F64");
+    if (mo) {
+        std::string e = dh::check_t2map(*mo);
+        if (!e.empty()) return fail(ctx, mo->legacy ? DECAES_ELEGACY : DECAES_EINVAL, e);
+    }
+    if (po) {
+        std::string e = dh::check_t2part(*po);
+        if (!e.empty()) return fail(ctx, po->legacy ? DECAES_ELEGACY : DECAES_EINVAL, e);
+        if (mo) {
+            if (po->nT2 != mo->nT2) return fail(ctx, DECAES_EINVAL, "T2part nT2 must equal T2map nT2");
+            for (int d = 0; d < 3; ++d)
+                if (po->MatrixSize[d] != mo->MatrixSize[d]) return fail(ctx, DECAES_EINVAL, "T2part MatrixSize must equal T2map MatrixSize");
+        }
+    }
+    return DECAES_OK;
+}
+
+void copy_constants(const decaes_t2map_opts &o, const Basis *B, decaes_t2map_out *out, int dtype, decaes_ctx *ctx) {
+    auto put = [&](void *dst, const std::vector<double> &v) {
+        if (!dst) return;
+        for (size_t i = 0; i < v.size(); ++i) {
+            if (dtype == DECAES_F32) ((float *)dst)[i] = (float)v[i];
+            else ((double *)dst)[i] = v[i];
+        }
+    };
+    std::vector<double> te(o.nTE);
+    for (int i = 0; i < o.nTE; ++i) te[i] = o.TE * (i + 1);
+    put(out->echotimes, te);
+    put(out->t2times, B->h_t2);
+    put(out->refangleset, B->h_angles);
+    const bool fixed = !std::isnan(o.SetFlipAngle);
+    size_t len = (size_t)o.nTE * o.nT2 * (fixed ? 1 : o.nRefAngles);
+    void *dsts[2] = {out->decaybasisset, fixed && o.SaveNNLSBasis ? out->decaybasis : nullptr};
+    std::vector<double> h;
+    for (void *dst : dsts) {
+        if (!dst) continue;
+        if (h.empty()) {
+            h.resize(len);
+            cudaMemcpyAsync(h.data(), fixed ? B->fixed : B->As, sizeof(double) * len, cudaMemcpyDeviceToHost, ctx->stream);
+            cudaStreamSynchronize(ctx->stream);
+        }
+        put(dst, h);
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" decaes_ctx *decaes_create(int device, size_t hbm_budget_bytes) {
+    auto *c = new decaes_ctx();
+    c->device = device;
+    c->budget = hbm_budget_bytes ? hbm_budget_bytes : (size_t)160 << 30;
+    if (cudaSetDevice(device) != cudaSuccess) { delete c; return nullptr; }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) { delete c; return nullptr; }
+    c->sms = prop.multiProcessorCount;
+    c->smem_optin = prop.sharedMemPerBlockOptin;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return nullptr; }
+    for (auto &e : c->ev) cudaEventCreate(&e);
+    return c;
+}
+
+extern "C" void decaes_destroy(decaes_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : ctx->bufs) cudaFree(kv.second.p);
+    for (auto &kv : ctx->bases) {
+        Basis &b = kv.second;
+        cudaFree(b.t2); cudaFree(b.logt2); cudaFree(b.angles); cudaFree(b.As); cudaFree(b.dAs); cudaFree(b.fixed);
+    }
+    for (auto &e : ctx->ev) cudaEventDestroy(e);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" const char *decaes_last_error(const decaes_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+extern "C" int decaes_get_stats(const decaes_ctx *ctx, decaes_stats *out) {
+    if (!ctx || !out) return DECAES_EINVAL;
+    *out = ctx->stats;
+    return DECAES_OK;
+}
+
+static int t2map_host(decaes_ctx *ctx, const decaes_t2map_opts *mo, const decaes_t2part_opts *po, const void *image,
+                      int dtype, const void *b1map, decaes_t2map_out *mout, decaes_t2part_out *pout) {
+    if (int rc = check_both(ctx, mo, po, dtype)) return rc;
+    if (!image || !mout) return fail(ctx, DECAES_EINVAL, "image and out must not be NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, DECAES_ECUDA, "cudaSetDevice failed");
+    const decaes_t2map_opts &o = *mo;
+    const long V = (long)o.MatrixSize[0] * o.MatrixSize[1] * o.MatrixSize[2];
+    cudaStream_t st = ctx->stream;
+    int launches = 0;
+    ctx->stats = decaes_stats{};
+    void *d_img, *d_b1 = nullptr;
+    size_t img_bytes = esize(dtype) * (size_t)V * o.nTE;
+    if (int rc = buf(ctx, "image", img_bytes, &d_img)) return rc;
+    if (b1map)
+        if (int rc = buf(ctx, "b1map", esize(dtype) * (size_t)V, &d_b1)) return rc;
+    OutMap om;
+    if (int rc = out_layout(ctx, o, pout != nullptr, om)) return rc;
+    CK(cudaEventRecord(ctx->ev[0], st));
+    CK(cudaMemcpyAsync(d_img, image, img_bytes, cudaMemcpyHostToDevice, st));
+    if (b1map) CK(cudaMemcpyAsync(d_b1, b1map, esize(dtype) * (size_t)V, cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(ctx->ev[1], st));
+    if (int rc = run_t2map(ctx, o, pout ? po : nullptr, d_img, dtype, d_b1, om, st, &launches)) return rc;
+    CK(cudaEventRecord(ctx->ev[4], st));
+    const size_t n = o.nT2, m = o.nTE;
+    struct { const double *s; void *d; size_t len; } cp[] = {
+        {om.dist, mout->dist, V * n}, {om.gdn, mout->gdn, (size_t)V}, {om.ggm, mout->ggm, (size_t)V},
+        {om.gva, mout->gva, (size_t)V}, {om.fnr, mout->fnr, (size_t)V}, {om.snr, mout->snr, (size_t)V},
+        {om.alpha, mout->alpha, (size_t)V}, {om.resnorm, mout->resnorm, (size_t)V}, {om.decaycurve, mout->decaycurve, V * m},
+        {om.mu, mout->mu, (size_t)V}, {om.chi2f, mout->chi2factor, (size_t)V}, {om.basis, mout->decaybasis, V * m * n},
+    };
+    for (auto &c : cp)
+        if (int rc = copy_out(ctx, c.s, c.d, c.len, dtype, st, &launches)) return rc;
+    if (pout) {
+        struct { const double *s; void *d; } pc[] = {{om.sfr, pout->sfr}, {om.sgm, pout->sgm}, {om.mfr, pout->mfr}, {om.mgm, pout->mgm}};
+        for (auto &c : pc)
+            if (int rc = copy_out(ctx, c.s, c.d, (size_t)V, dtype, st, &launches)) return rc;
+    }
+    CK(cudaEventRecord(ctx->ev[5], st));
+    CK(cudaStreamSynchronize(st));
+    Basis *B;
+    if (int rc = get_basis(ctx, o, &B)) return rc;
+    copy_constants(o, B, mout, dtype, ctx);
+    unsigned long long hs[2];
+    int hn;
+    void *cnt;
+    buf(ctx, "counters", 64, &cnt);
+    CK(cudaMemcpy(&hn, cnt, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hs, (char *)cnt + 16, sizeof hs, cudaMemcpyDeviceToHost));
+    float t;
+    decaes_stats &S = ctx->stats;
+    S.voxels = V;
+    S.voxels_processed = hn;
+    S.nnls_cap_hits = (int64_t)hs[0];
+    S.search_limit_hits = (int64_t)hs[1];
+    cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[5]); S.ms_total = t;
+    cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]); S.ms_solve = t;
+    cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]); S.ms_h2d = t;
+    cudaEventElapsedTime(&t, ctx->ev[4], ctx->ev[5]); S.ms_d2h = t;
+    S.solve_launches = 1;
+    S.kernel_launches = launches;
+    return DECAES_OK;
+}
+
+extern "C" int decaes_t2map(decaes_ctx *ctx, const decaes_t2map_opts *opts, const void *image, int dtype,
+                            const void *b1map, decaes_t2map_out *out) {
+    return t2map_host(ctx, opts, nullptr, image, dtype, b1map, out, nullptr);
+}
+
+extern "C" int decaes_t2map_t2part(decaes_ctx *ctx, const decaes_t2map_opts *mopts, const decaes_t2part_opts *popts,
+                                   const void *image, int dtype, const void *b1map, decaes_t2map_out *mout,
+                                   decaes_t2part_out *pout) {
+    if (!popts || !pout) return fail(ctx, DECAES_EINVAL, "T2part options and outputs must not be NULL");
+    return t2map_host(ctx, mopts, popts, image, dtype, b1map, mout, pout);
+}
+
+extern "C" int decaes_t2map_t2part_device(decaes_ctx *ctx, const decaes_t2map_opts *mopts, const decaes_t2part_opts *popts,
+                                          const void *d_image, int dtype, const void *d_b1map, decaes_t2map_out *d_mout,
+                                          decaes_t2part_out *d_pout, void *stream) {
+    if (int rc = check_both(ctx, mopts, popts, dtype)) return rc;
+    if (dtype != DECAES_F64 && dtype != DECAES_F32) return fail(ctx, DECAES_EINVAL, "bad dtype");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    const decaes_t2map_opts &o = *mopts;
+    const long V = (long)o.MatrixSize[0] * o.MatrixSize[1] * o.MatrixSize[2];
+    int launches = 0;
+    ctx->stats = decaes_stats{};
+    OutMap om;
+    if (int rc = out_layout(ctx, o, d_pout != nullptr, om)) return rc;
+    CK(cudaEventRecord(ctx->ev[0], st));
+    if (int rc = run_t2map(ctx, o, d_pout ? popts : nullptr, d_image, dtype, d_b1map, om, st, &launches)) return rc;
+    // hand results to the caller's device buffers (double outputs: plain device copies;
+    // float outputs: narrowing kernel)
+    const size_t n = o.nT2, m = o.nTE;
+    struct { const double *s; void *d; size_t len; } cp[] = {
+        {om.dist, d_mout->dist, V * n}, {om.gdn, d_mout->gdn, (size_t)V}, {om.ggm, d_mout->ggm, (size_t)V},
+        {om.gva, d_mout->gva, (size_t)V}, {om.fnr, d_mout->fnr, (size_t)V}, {om.snr, d_mout->snr, (size_t)V},
+        {om.alpha, d_mout->alpha, (size_t)V}, {om.resnorm, d_mout->resnorm, (size_t)V},
+        {om.decaycurve, d_mout->decaycurve, V * m}, {om.mu, d_mout->mu, (size_t)V}, {om.chi2f, d_mout->chi2factor, (size_t)V},
+        {om.basis, d_mout->decaybasis, V * m * n},
+        {om.sfr, d_pout ? d_pout->sfr : nullptr, (size_t)V}, {om.sgm, d_pout ? d_pout->sgm : nullptr, (size_t)V},
+        {om.mfr, d_pout ? d_pout->mfr : nullptr, (size_t)V}, {om.mgm, d_pout ? d_pout->mgm : nullptr, (size_t)V},
+    };
+    for (auto &c : cp) {
+        if (!c.s || !c.d) continue;
+        if (dtype == DECAES_F64) {
+            CK(cudaMemcpyAsync(c.d, c.s, sizeof(double) * c.len, cudaMemcpyDeviceToDevice, st));
+        } else {
+            int g = (int)std::min<long>(8L * ctx->sms, ((long)c.len + 255) / 256);
+            dk::k_narrow<<<std::max(g, 1), 256, 0, st>>>(c.s, (float *)c.d, (long)c.len);
+            ++launches;
+        }
+    }
+    CK(cudaEventRecord(ctx->ev[5], st));
+    CK(cudaGetLastError());
+    ctx->stats.voxels = V;
+    ctx->stats.solve_launches = 1;
+    ctx->stats.kernel_launches = launches;
+    return DECAES_OK;
+}
+
+// Completes the statistics of the last device-pointer call (synchronizes its stream).
+extern "C" int decaes_sync_stats(decaes_ctx *ctx, void *stream) {
+    if (!ctx) return DECAES_EINVAL;
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    CK(cudaStreamSynchronize(st));
+    void *cnt;
+    if (int rc = buf(ctx, "counters", 64, &cnt)) return rc;
+    int hn;
+    unsigned long long hs[2];
+    CK(cudaMemcpy(&hn, cnt, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hs, (char *)cnt + 16, sizeof hs, cudaMemcpyDeviceToHost));
+    float t;
+    ctx->stats.voxels_processed = hn;
+    ctx->stats.nnls_cap_hits = (int64_t)hs[0];
+    ctx->stats.search_limit_hits = (int64_t)hs[1];
+    cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[5]); ctx->stats.ms_total = t;
+    cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]); ctx->stats.ms_solve = t;
+    return DECAES_OK;
+}
+
+extern "C" int decaes_t2part(decaes_ctx *ctx, const decaes_t2part_opts *opts, const void *dist, int dtype,
+                             decaes_t2part_out *out) {
+    if (int rc = check_both(ctx, nullptr, opts, dtype)) return rc;
+    if (!dist || !out) return fail(ctx, DECAES_EINVAL, "dist and out must not be NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    const decaes_t2part_opts &o = *opts;
+    const long V = (long)o.MatrixSize[0] * o.MatrixSize[1] * o.MatrixSize[2];
+    const int n = o.nT2;
+    dh::T2partPlan pp{};
+    std::string e = dh::t2part_plan(o, pp);
+    if (!e.empty()) return fail(ctx, DECAES_EINVAL, e);
+    cudaStream_t st = ctx->stream;
+    int launches = 0;
+    ctx->stats = decaes_stats{};
+    void *d_dist, *d_out, *d_lt, *d_w = nullptr;
+    if (int rc = buf(ctx, "t2p_dist", esize(dtype) * (size_t)V * n, &d_dist)) return rc;
+    if (int rc = buf(ctx, "t2p_out", sizeof(double) * 4 * (size_t)V, &d_out)) return rc;
+    if (int rc = buf(ctx, "t2p_logt2", sizeof(double) * n, &d_lt)) return rc;
+    if (!pp.weights.empty())
+        if (int rc = buf(ctx, "t2p_w", sizeof(double) * n, &d_w)) return rc;
+    CK(cudaEventRecord(ctx->ev[0], st));
+    CK(cudaMemcpyAsync(d_dist, dist, esize(dtype) * (size_t)V * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_lt, pp.logt2.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    if (d_w) CK(cudaMemcpyAsync(d_w, pp.weights.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    double *po = (double *)d_out;
+    {
+        int g = (int)std::min<long>(8L * ctx->sms, (4 * V + 255) / 256);
+        dk::k_fill<<<std::max(g, 1), 256, 0, st>>>(po, 4 * V, NAN);
+        ++launches;
+    }
+    int g = (int)std::min<long>(8L * ctx->sms, (V + 127) / 128);
+    if (dtype == DECAES_F32)
+        dk::k_t2part<float><<<std::max(g, 1), 128, 0, st>>>((const float *)d_dist, V, n, pp.sp0, pp.sp1, pp.mp0, pp.mp1,
+                                                             (const double *)d_lt, (const double *)d_w, po, po + V, po + 2 * V, po + 3 * V);
+    else
+        dk::k_t2part<double><<<std::max(g, 1), 128, 0, st>>>((const double *)d_dist, V, n, pp.sp0, pp.sp1, pp.mp0, pp.mp1,
+                                                              (const double *)d_lt, (const double *)d_w, po, po + V, po + 2 * V, po + 3 * V);
+    ++launches;
+    CK(cudaGetLastError());
+    void *dsts[4] = {out->sfr, out->sgm, out->mfr, out->mgm};
+    for (int k = 0; k < 4; ++k)
+        if (int rc = copy_out(ctx, po + k * V, dsts[k], (size_t)V, dtype, st, &launches)) return rc;
+    CK(cudaEventRecord(ctx->ev[5], st));
+    CK(cudaStreamSynchronize(st));
+    float t;
+    cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[5]);
+    ctx->stats.voxels = V;
+    ctx->stats.ms_total = t;
+    ctx->stats.kernel_launches = launches;
+    return DECAES_OK;
+}

@@ -1,0 +1,917 @@
+// t2map_device.cuh -- per-voxel pipeline of T2mapSEcorr on one warp:
+// normalization, flip-angle search, EPG basis, regularized NNLS and the
+// save_results!/T2part epilogue (src/T2mapSEcorr.jl:201-238, 409-591;
+// src/lsqnonneg.jl; src/splines.jl; src/optimization.jl; src/T2partSEcorr.jl).
+#pragma once
+#include "epg.cuh"
+#include "nnls_warp.cuh"
+
+namespace dk {
+
+constexpr int kCacheCap = 128;   // L-curve cache entries per voxel (the loop needs ~30)
+constexpr int kLoopCap = 512;    // hard cap of every data-dependent outer loop
+
+struct Params {
+    int m, n, K, M, lda;
+    int reg;
+    double chi2factor, noiselevel;
+    int mineval, maxeval;
+    int angle_mode;  // 0 search, 1 fixed SetFlipAngle, 2 B1 map
+    double fixed_angle;
+    int beta180;
+    double beta, TE, T1;
+    long V;
+    const int *nvox;
+    const int *vidx;
+    const void *image;
+    int image_f32;
+    const void *b1map;
+    const double *t2, *logt2, *angles, *As, *dAs, *basis_fixed;
+    double *scratch;
+    long scr_stride;  // doubles per warp
+    int *counter;
+    unsigned long long *stats;  // [0] NNLS cap hits, [1] loop cap hits
+    double *dist, *gdn, *ggm, *gva, *fnr, *snr, *alpha, *resnorm, *decaycurve, *mu, *chi2f, *basis_out;
+    int fuse_t2part, sp0, sp1, mp0, mp1;
+    const double *weights;
+    double *sfr, *sgm, *mfr, *mgm;
+    int need_chi2;
+    int epg_lanes;
+};
+
+// Shared-memory footprint of one warp worker (doubles), mirrored on the host.
+__host__ __device__ inline long warp_smem_doubles(int m, int n, int lda) {
+    long d = (long)lda * n + 3L * lda + 3L * n + 8;
+    long ints = 2L * n;            // idx
+    long bytes = (long)n;          // diag
+    return d + (ints * 4 + bytes + 7) / 8;
+}
+// Global scratch of one warp worker (doubles).
+__host__ __device__ inline long warp_scratch_doubles(int m, int n, int K) {
+    int mn = m < n ? m : n;
+    return (long)m * n + 3L * K + (long)kCacheCap * (3 + 4 + 12) + mn + 16;
+}
+
+struct Warp {
+    const Params *P;
+    NnlsWS s;
+    double *data;  // normalized decay data (shared), m
+    double *xout;  // saved solution (shared), n
+    double *A;     // per-voxel basis (global scratch), m x n
+    double *scr;   // per-warp global scratch base
+    int lane;
+    unsigned nnls_caps, loop_caps;
+};
+
+__device__ __forceinline__ void note(Warp &w, const NnlsResult &r) { w.nnls_caps += (r.mode != 0); }
+
+// ----------------------------------------------------------------------------
+// Tikhonov helpers (src/lsqnonneg.jl:297-318)
+// ----------------------------------------------------------------------------
+struct TikhState {
+    NnlsResult r;
+    double mu;
+};
+__device__ TikhState tikh_solve(Warp &w, double mu) {
+    TikhState t;
+    t.r = warp_lsq(w.s, w.A, w.P->m, w.P->n, w.data, true, mu);
+    t.mu = mu;
+    note(w, t.r);
+    return t;
+}
+__device__ double tikh_res2(Warp &w, const TikhState &t) {
+    double ssq = warp_seminorm_sq(w.s, t.r.nsetp);
+    return jmax(__dsub_rn(__dmul_rn(t.r.rnorm, t.r.rnorm), __dmul_rn(__dmul_rn(t.mu, t.mu), ssq)), 0.0);
+}
+__device__ void save_x(Warp &w) {
+    for (int j = w.lane; j < w.P->n; j += 32) w.xout[j] = w.s.x[j];
+    __syncwarp();
+}
+
+// ----------------------------------------------------------------------------
+// Root finding and minimization (src/optimization.jl)
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ double jsign(double x) { return x < 0 ? -1.0 : (x > 0 ? 1.0 : x); }
+
+// bracket_root_monotonic, src/optimization.jl:191-219
+template <class F>
+__device__ void bracket_root_monotonic(F &f, double a, double delta, double dilate, double mono, int maxiters, double &ra,
+                                       double &rb, double &rfa, double &rfb) {
+    double fa = f(a);
+    if (!isfinite(fa)) { ra = rb = a; rfa = rfb = CUDART_NAN; return; }
+    if (fa == 0) { ra = rb = a; rfa = rfb = fa; return; }
+    double sgn = jsign(mono) * jsign(fa);
+    double b = a - sgn * delta;
+    double fb = f(b);
+    if (!isfinite(fb)) { ra = rb = a; rfa = rfb = fa; return; }
+    if (fb == 0) { ra = rb = b; rfa = rfb = fb; return; }
+    delta *= dilate;
+    int cnt = 0;
+    while (fa * fb > 0 && cnt < maxiters) {
+        a = b; fa = fb;
+        b = a - sgn * delta;
+        fb = f(b);
+        if (!isfinite(fb)) { ra = rb = a; rfa = rfb = fa; return; }
+        if (fb == 0) { ra = rb = b; rfa = rfb = fb; return; }
+        delta *= dilate;
+        cnt += 1;
+    }
+    if (a < b) { ra = a; rb = b; rfa = fa; rfb = fb; }
+    else { ra = b; rb = a; rfa = fb; rfb = fa; }
+}
+
+// brent_root, src/optimization.jl:71-128
+template <class F>
+__device__ void brent_root(F &f, double x0, double x1, double fx0, double fx1, double xatol, double xrtol, double ftol,
+                           int maxiters, double &xr, double &fxr) {
+    if (fx0 == 0) { xr = x0; fxr = fx0; return; }
+    if (fx1 == 0) { xr = x1; fxr = fx1; return; }
+    double a = x0, b = x1, fa = fx0, fb = fx1;
+    if (fabs(fa) < fabs(fb)) { double t = a; a = b; b = t; t = fa; fa = fb; fb = t; }
+    double c = x0, d = x0, fc = fx0;
+    bool mflag = true;
+    for (int iter = 1; iter <= maxiters; ++iter) {
+        if (fabs(b - a) <= 2 * (xatol + xrtol * fabs(b))) { xr = b; fxr = fb; return; }
+        double s = 0;
+        s += a * fb * fc / (fa - fb) / (fa - fc);
+        s += b * fa * fc / (fb - fa) / (fb - fc);
+        s += c * fa * fb / (fc - fa) / (fc - fb);
+        if (isnan(s) || isinf(s)) s = a - fa * (b - a) / (fb - fa);
+        double u = (3 * a + b) / 4, v = b;
+        if (u > v) { double t = u; u = v; v = t; }
+        double tol = jmax(xatol, xrtol * jmax(jmax(fabs(b), fabs(c)), fabs(d)));
+        if (!(u < s && s < v) || (mflag && fabs(s - b) >= fabs(b - c) / 2) || (!mflag && fabs(s - b) >= fabs(b - c) / 2) ||
+            (mflag && fabs(b - c) <= tol) || (!mflag && fabs(c - d) <= tol)) {
+            s = (a + b) / 2;
+            mflag = true;
+        } else {
+            mflag = false;
+        }
+        double fs = f(s);
+        if (fs == 0) { xr = s; fxr = fs; return; }
+        if (isnan(fs) || isinf(fs)) { xr = b; fxr = fb; return; }
+        if (fabs(fs) <= ftol) { xr = s; fxr = fs; return; }
+        d = c; c = b; fc = fb;
+        if (jsign(fa) * jsign(fs) < 0) { b = s; fb = fs; }
+        else { a = s; fa = fs; }
+        if (fabs(fa) < fabs(fb)) { double t = a; a = b; b = t; t = fa; fa = fb; fb = t; }
+    }
+    xr = b;
+    fxr = fb;
+}
+
+// brent_minimize, src/optimization.jl:319-413
+template <class F>
+__device__ void brent_minimize(F &f, double x1, double x2, double xrtol, double xatol, int maxiters, double &xo, double &yo) {
+    const double PHI = 1.6180339887498949;
+    const double alpha = 2 - PHI;
+    double x = x1 + alpha * (x2 - x1);
+    double y = f(x);
+    double dx_old = 0, dx = 0, x_older = x, x_old = x, y_older = y, y_old = y;
+    int iter = 0;
+    while (iter < maxiters) {
+        double p = 0, q = 0, xm = (x2 + x1) / 2, tolx = xatol + xrtol * fabs(x);
+        if (fabs(x - xm) + (x2 - x1) / 2 <= 2 * tolx) break;
+        iter += 1;
+        if (fabs(dx_old) > tolx) {
+            double r = (x - x_old) * (y - y_older);
+            q = (x - x_older) * (y - y_old);
+            p = (x - x_older) * q - (x - x_old) * r;
+            q = 2 * (q - r);
+            if (q > 0) p = -p;
+            else q = -q;
+        }
+        if (fabs(p) < fabs(q * dx_old / 2) && p < q * (x2 - x) && p < q * (x - x1)) {
+            dx_old = dx;
+            dx = p / q;
+            double xt = x + dx;
+            if ((xt - x1) < 2 * tolx || (x2 - xt) < 2 * tolx) dx = (x < xm) ? tolx : -tolx;
+        } else {
+            dx_old = (x < xm) ? x2 - x : x1 - x;
+            dx = alpha * dx_old;
+        }
+        double x_new = (fabs(dx) >= tolx) ? x + dx : x + ((dx > 0) ? tolx : -tolx);
+        double y_new = f(x_new);
+        if (y_new < y) {
+            if (x_new < x) x2 = x; else x1 = x;
+            x_older = x_old; x_old = x; x = x_new;
+            y_older = y_old; y_old = y; y = y_new;
+        } else {
+            if (x_new < x) x1 = x_new; else x2 = x_new;
+            if (y_new <= y_old || x_old == x) {
+                x_older = x_old; x_old = x_new;
+                y_older = y_old; y_old = y_new;
+            } else if (y_new <= y_older || x_older == x || x_older == x_old) {
+                x_older = x_new;
+                y_older = y_new;
+            }
+        }
+    }
+    xo = x;
+    yo = y;
+}
+
+// ----------------------------------------------------------------------------
+// Regularizers (src/lsqnonneg.jl:504-1341)
+// ----------------------------------------------------------------------------
+struct Chi2F {  // f(logμ) of lsqnonneg_chi2!, src/lsqnonneg.jl:566-569
+    Warp *w;
+    double target;
+    __device__ double operator()(double logmu) {
+        TikhState t = tikh_solve(*w, exp(logmu));
+        return (tikh_res2(*w, t) - target) / target;
+    }
+};
+struct MdpF {  // f(logμ) of lsqnonneg_mdp!, src/lsqnonneg.jl:723-726
+    Warp *w;
+    double delta2;
+    __device__ double operator()(double logmu) {
+        TikhState t = tikh_solve(*w, exp(logmu));
+        return tikh_res2(*w, t) - delta2;
+    }
+};
+
+// lsqnonneg_chi2! (method :brent), src/lsqnonneg.jl:504-593.  The solution
+// that save_results! stores ends up in w.xout.  On the early exit the
+// reference saves its smoothing cache's stale slot; x_unreg is stored here.
+__device__ void reg_chi2(Warp &w, double chi2_target, double &mu_out, double &chi2_out) {
+    const Params &P = *w.P;
+    NnlsResult r0 = warp_lsq(w.s, w.A, P.m, P.n, w.data, false, 0.0);
+    note(w, r0);
+    double res2_min = __dmul_rn(r0.rnorm, r0.rnorm);
+    if (res2_min == 0 || r0.nsetp == 0) {
+        save_x(w);
+        mu_out = 0; chi2_out = 1;
+        return;
+    }
+    Chi2F f{&w, chi2_target * res2_min};
+    double a, b, fa, fb, logmu, relerr;
+    bracket_root_monotonic(f, -4.0, 1.0, 1.5, 1.0, 6, a, b, fa, fb);
+    if (fa * fb < 0) {
+        brent_root(f, a, b, fa, fb, 0.0, 0.0, 1e-3 * (chi2_target - 1), 100, logmu, relerr);
+    } else {
+        if (!isfinite(fa)) { logmu = b; relerr = fb; }
+        else if (!isfinite(fb)) { logmu = a; relerr = fa; }
+        else if (fabs(fa) < fabs(fb)) { logmu = a; relerr = fa; }
+        else { logmu = b; relerr = fb; }
+    }
+    double mu, res2;
+    if (isfinite(relerr)) {
+        mu = exp(logmu);
+        res2 = f.target * (1 + relerr);
+        tikh_solve(w, mu);
+    } else {
+        mu = 0; res2 = 1;  // saved solution: the last Tikhonov solve
+    }
+    save_x(w);
+    mu_out = mu;
+    chi2_out = res2 / res2_min;
+}
+
+// lsqnonneg_mdp!, src/lsqnonneg.jl:700-747.  Early exits store the returned
+// x (x_unreg or zeros) where the reference saves a stale cache slot.
+__device__ void reg_mdp(Warp &w, double delta, double &mu_out, double &chi2_out) {
+    const Params &P = *w.P;
+    NnlsResult r0 = warp_lsq(w.s, w.A, P.m, P.n, w.data, false, 0.0);
+    note(w, r0);
+    double res2_min = __dmul_rn(r0.rnorm, r0.rnorm);
+    if (delta <= sqrt(res2_min)) { save_x(w); mu_out = 0; chi2_out = 1; return; }
+    double part = 0;
+    for (int i = w.lane; i < P.m; i += 32) part = __dadd_rn(part, __dmul_rn(w.data[i], w.data[i]));
+    double res2_max = wsum(part);
+    if (delta >= sqrt(res2_max)) {
+        for (int j = w.lane; j < P.n; j += 32) w.xout[j] = 0.0;
+        __syncwarp();
+        mu_out = CUDART_INF; chi2_out = res2_max / res2_min;
+        return;
+    }
+    MdpF f{&w, delta * delta};
+    double a, b, fa, fb, logmu, err;
+    bracket_root_monotonic(f, -4.0, 1.0, 1.5, 1.0, 6, a, b, fa, fb);
+    if (fa * fb < 0) {
+        brent_root(f, a, b, fa, fb, 0.0, 0.0, 1e-3 * (delta * delta), 100, logmu, err);
+    } else {
+        if (!isfinite(fa)) { logmu = b; err = fb; }
+        else if (!isfinite(fb)) { logmu = a; err = fa; }
+        else if (fabs(fa) < fabs(fb)) { logmu = a; err = fa; }
+        else { logmu = b; err = fb; }
+    }
+    double mu, res2;
+    if (isfinite(err)) {
+        mu = exp(logmu);
+        res2 = delta * delta + err;
+        tikh_solve(w, mu);
+    } else {
+        mu = 0; res2 = 1;
+    }
+    save_x(w);
+    mu_out = mu;
+    chi2_out = res2 / res2_min;
+}
+
+// ---- L-curve corner (src/lsqnonneg.jl:812-972), caches in global scratch ----
+struct LCurve {
+    Warp *w;
+    double *fx, *fP;          // CachedFunction: keys, values (isapprox keys)
+    double *px, *pP, *pC;     // point cache
+    double *sx, *sP;          // state cache
+    int flen, plen, slen;
+    bool overflow;
+};
+__device__ __forceinline__ bool isapprox(double x, double y) {
+    if (x == y) return true;
+    if (!(isfinite(x) && isfinite(y))) return false;
+    return fabs(x - y) <= jmax(0.0, 1.4901161193847656e-08 * jmax(fabs(x), fabs(y)));
+}
+__device__ __forceinline__ bool jisless(double a, double b) {
+    if (isnan(a)) return false;
+    if (isnan(b)) return true;
+    if (a == b) return signbit(a) && !signbit(b);
+    return a < b;
+}
+// f_lcurve(logμ) = (log ||Ax-b||^2, log ||x||^2) through the isapprox-keyed cache
+__device__ void lc_eval(LCurve &L, double x, double &P0, double &P1) {
+    for (int i = 0; i < L.flen; ++i)
+        if (isapprox(x, L.fx[i])) { P0 = L.fP[2 * i]; P1 = L.fP[2 * i + 1]; return; }
+    Warp &w = *L.w;
+    TikhState t = tikh_solve(w, exp(x));
+    double res2 = tikh_res2(w, t);
+    double ssq = warp_seminorm_sq(w.s, t.r.nsetp);
+    P0 = log(res2);
+    P1 = log(ssq);
+    if (L.flen < kCacheCap) {
+        if (w.lane == 0) { L.fx[L.flen] = x; L.fP[2 * L.flen] = P0; L.fP[2 * L.flen + 1] = P1; }
+        __syncwarp();
+        L.flen++;
+    } else {
+        L.overflow = true;
+    }
+}
+__device__ int pc_find(const LCurve &L, double x) {
+    for (int i = 0; i < L.plen; ++i) if (isapprox(x, L.px[i])) return i;
+    return -1;
+}
+__device__ void pc_set(LCurve &L, double x, double P0, double P1, double C, bool push_only) {
+    int i = push_only ? -1 : pc_find(L, x);
+    if (i < 0) {
+        if (L.plen >= kCacheCap) { L.overflow = true; return; }
+        i = L.plen++;
+        if (L.w->lane == 0) L.px[i] = x;
+    }
+    if (L.w->lane == 0) { L.pP[2 * i] = P0; L.pP[2 * i + 1] = P1; L.pC[i] = C; }
+    __syncwarp();
+}
+__device__ int pc_argmax(const LCurve &L) {
+    int im = 0;
+    for (int i = 1; i < L.plen; ++i) if (jisless(L.pC[im], L.pC[i])) im = i;
+    return im;
+}
+__device__ __forceinline__ double nrm2(double a, double b) { return sqrt(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b))); }
+__device__ double menger(double j0, double j1, double k0, double k1, double l0, double l1) {
+    double djk0 = j0 - k0, djk1 = j1 - k1, dkl0 = k0 - l0, dkl1 = k1 - l1, dlj0 = l0 - j0, dlj1 = l1 - j1;
+    double a = __dadd_rn(__dmul_rn(djk0, djk0), __dmul_rn(djk1, djk1));
+    double b = __dadd_rn(__dmul_rn(dkl0, dkl0), __dmul_rn(dkl1, dkl1));
+    double c = __dadd_rn(__dmul_rn(dlj0, dlj0), __dmul_rn(dlj1, dlj1));
+    double cr = __dsub_rn(__dmul_rn(djk0, dkl1), __dmul_rn(djk1, dkl0));
+    return 2 * cr / sqrt(__dmul_rn(__dmul_rn(a, b), c));
+}
+struct LcState {
+    double x[4], P[8];
+};
+// update_curvature!, src/lsqnonneg.jl:948-965
+__device__ void lc_update_curvature(LCurve &L, const LcState &s, const double *Ptl, const double *Pbr, double Ctol) {
+    for (int i = 0; i < 4; ++i) {
+        double x = s.x[i], P0 = s.P[2 * i], P1 = s.P[2 * i + 1];
+        double C = -CUDART_INF;
+        if (jmin(nrm2(P0 - Ptl[0], P1 - Ptl[1]), nrm2(P0 - Pbr[0], P1 - Pbr[1])) > Ctol) {
+            double xm = -CUDART_INF, xp = CUDART_INF, m0 = P0, m1 = P1, p0 = P0, p1 = P1;
+            for (int k = 0; k < L.plen; ++k) {
+                double xk = L.px[k];
+                if (xm < xk && xk < x) { xm = xk; m0 = L.pP[2 * k]; m1 = L.pP[2 * k + 1]; }
+                if (x < xk && xk < xp) { xp = xk; p0 = L.pP[2 * k]; p1 = L.pP[2 * k + 1]; }
+            }
+            C = menger(m0, m1, P0, P1, p0, p1);
+        }
+        pc_set(L, x, P0, P1, C, false);
+    }
+}
+// lcurve_corner with backtracking, src/lsqnonneg.jl:872-919
+__device__ double lcurve_corner(LCurve &L, double xlow, double xhigh, double xtol, double Ptol, double Ctol) {
+    const double PHI = 1.6180339887498949;
+    L.flen = L.plen = L.slen = 0;
+    L.overflow = false;
+    LcState st;
+    st.x[0] = xlow;
+    st.x[3] = xhigh;
+    st.x[1] = (PHI * st.x[0] + st.x[3]) / (PHI + 1);
+    st.x[2] = st.x[0] + (st.x[3] - st.x[1]);
+    for (int i = 0; i < 4; ++i) lc_eval(L, st.x[i], st.P[2 * i], st.P[2 * i + 1]);
+    for (int i = 0; i < 4; ++i) pc_set(L, st.x[i], st.P[2 * i], st.P[2 * i + 1], -CUDART_INF, true);
+    double Ptl[2] = {st.P[0], st.P[1]}, Pbr[2] = {st.P[6], st.P[7]};
+    lc_update_curvature(L, st, Ptl, Pbr, Ctol);
+    int iter = 0;
+    while (!(fabs(st.x[3] - st.x[0]) < xtol || nrm2(st.P[0] - st.P[6], st.P[1] - st.P[7]) < Ptol)) {
+        iter += 1;
+        if (iter > kLoopCap || L.overflow) { L.w->loop_caps++; break; }
+        double xb = L.px[pc_argmax(L)];
+        for (int k = 0; k < L.slen; ++k) {
+            const double *sx = L.sx + 4 * k;
+            if ((sx[1] == xb || sx[2] == xb) && fabs(sx[3] - sx[0]) <= fabs(st.x[3] - st.x[0])) {
+                for (int q = 0; q < 4; ++q) st.x[q] = sx[q];
+                for (int q = 0; q < 8; ++q) st.P[q] = L.sP[8 * k + q];
+            }
+        }
+        int i2 = pc_find(L, st.x[1]), i3 = pc_find(L, st.x[2]);
+        if (i2 < 0 || i3 < 0) { L.w->loop_caps++; break; }
+        LcState ns;
+        if (L.pC[i2] > L.pC[i3]) {  // move_left
+            ns.x[0] = st.x[0]; ns.x[1] = (PHI * st.x[0] + st.x[2]) / (PHI + 1); ns.x[2] = st.x[1]; ns.x[3] = st.x[2];
+            ns.P[0] = st.P[0]; ns.P[1] = st.P[1];
+            lc_eval(L, ns.x[1], ns.P[2], ns.P[3]);
+            ns.P[4] = st.P[2]; ns.P[5] = st.P[3]; ns.P[6] = st.P[4]; ns.P[7] = st.P[5];
+        } else {  // move_right
+            ns.x[0] = st.x[1]; ns.x[1] = st.x[2]; ns.x[2] = st.x[1] + (st.x[3] - st.x[2]); ns.x[3] = st.x[3];
+            ns.P[0] = st.P[2]; ns.P[1] = st.P[3]; ns.P[2] = st.P[4]; ns.P[3] = st.P[5];
+            lc_eval(L, ns.x[2], ns.P[4], ns.P[5]);
+            ns.P[6] = st.P[6]; ns.P[7] = st.P[7];
+        }
+        st = ns;
+        lc_update_curvature(L, st, Ptl, Pbr, Ctol);
+        if (L.slen < kCacheCap) {
+            if (L.w->lane == 0) {
+                for (int q = 0; q < 4; ++q) L.sx[4 * L.slen + q] = st.x[q];
+                for (int q = 0; q < 8; ++q) L.sP[8 * L.slen + q] = st.P[q];
+            }
+            __syncwarp();
+            L.slen++;
+        } else {
+            L.overflow = true;
+        }
+    }
+    return L.px[pc_argmax(L)];
+}
+
+__device__ double *lcurve_scratch(Warp &w) { return w.scr + (long)w.P->m * w.P->n + 3L * w.P->K; }
+
+// lsqnonneg_lcurve!, src/lsqnonneg.jl:812-840
+__device__ void reg_lcurve(Warp &w, double &mu_out, double &chi2_out) {
+    double *base = lcurve_scratch(w);
+    LCurve L;
+    L.w = &w;
+    L.fx = base; L.fP = L.fx + kCacheCap;
+    L.px = L.fP + 2 * kCacheCap; L.pP = L.px + kCacheCap; L.pC = L.pP + 2 * kCacheCap;
+    L.sx = L.pC + kCacheCap; L.sP = L.sx + 4 * kCacheCap;
+    double logmu = lcurve_corner(L, -8.0, 2.0, 1e-4, 1e-4, 1e-4);
+    double mu = exp(logmu);
+    TikhState t = tikh_solve(w, mu);
+    double res2 = tikh_res2(w, t);
+    save_x(w);
+    double chi2 = CUDART_NAN;
+    if (w.P->need_chi2) {
+        NnlsResult r0 = warp_lsq(w.s, w.A, w.P->m, w.P->n, w.data, false, 0.0);
+        note(w, r0);
+        chi2 = res2 / __dmul_rn(r0.rnorm, r0.rnorm);
+    }
+    mu_out = mu;
+    chi2_out = chi2;
+}
+
+// ---- GCV (src/lsqnonneg.jl:1136-1341) ----
+// Singular values of the m x n basis by one-sided Hestenes-Jacobi in shared
+// memory (stand-in for LAPACK dgesdd job 'N'), sorted descending into gam.
+__device__ void warp_svdvals(Warp &w, double *gam) {
+    const Params &P = *w.P;
+    const int m = P.m, n = P.n, lane = w.lane;
+    const int r = m >= n ? m : n, c = m >= n ? n : m;
+    const int ld = r | 1;
+    double *U = w.s.C;  // r x c, ld, fits in the lda x n workspace
+    for (int j = 0; j < c; ++j)
+        for (int i = lane; i < r; i += 32) U[i + (long)j * ld] = (m >= n) ? w.A[i + (long)j * m] : w.A[j + (long)i * m];
+    __syncwarp();
+    const double EPS = 2.220446049250313e-16;
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0;
+        for (int p = 0; p < c - 1; ++p) {
+            for (int q = p + 1; q < c; ++q) {
+                double *up = U + (long)p * ld, *uq = U + (long)q * ld;
+                double pa = 0, pb = 0, pg = 0;
+                for (int i = lane; i < r; i += 32) {
+                    double x = up[i], y = uq[i];
+                    pa = fma(x, x, pa); pb = fma(y, y, pb); pg = fma(x, y, pg);
+                }
+                double al = wsum(pa), be = wsum(pb), ga = wsum(pg);
+                if (ga == 0 || fabs(ga) <= EPS * sqrt(al * be)) continue;
+                double rel = fabs(ga) / sqrt(al * be);
+                off = rel > off ? rel : off;
+                double zeta = (be - al) / (2 * ga);
+                double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1 + zeta * zeta));
+                double cs = 1 / sqrt(1 + t * t), sn = cs * t;
+                for (int i = lane; i < r; i += 32) {
+                    double x = up[i], y = uq[i];
+                    up[i] = cs * x - sn * y;
+                    uq[i] = sn * x + cs * y;
+                }
+                __syncwarp();
+            }
+        }
+        if (off <= EPS) break;
+    }
+    // column norms, then rank-sort descending
+    double *tmp = w.s.zz;
+    for (int j = 0; j < c; ++j) {
+        const double *u = U + (long)j * ld;
+        double part = 0;
+        for (int i = lane; i < r; i += 32) part = fma(u[i], u[i], part);
+        double sv = sqrt(wsum(part));
+        if (lane == 0) tmp[j] = sv;
+    }
+    __syncwarp();
+    for (int j = lane; j < c; j += 32) {
+        double v = tmp[j];
+        int rank = 0;
+        for (int k = 0; k < c; ++k) rank += (tmp[k] > v) || (tmp[k] == v && k < j);
+        gam[rank] = v;
+    }
+    __syncwarp();
+}
+struct GcvF {  // log𝒢(logμ), src/lsqnonneg.jl:1150-1154 and gcv!, 1213-1229
+    Warp *w;
+    const double *gam;
+    double low;
+    __device__ double operator()(double logmu) {
+        const Params &P = *w->P;
+        double mu = exp(logmu);
+        TikhState t = tikh_solve(*w, mu);
+        double res2 = tikh_res2(*w, t);
+        int k = P.m < P.n ? P.m : P.n;
+        double dof = (double)(P.m - P.n > 0 ? P.m - P.n : 0), l2 = mu * mu;
+        for (int i = 0; i < k; ++i) { double g2 = gam[i] * gam[i]; dof += l2 / (g2 + l2); }
+        double G = res2 / (dof * dof);
+        return log(jmax(G, low));
+    }
+};
+__device__ void reg_gcv(Warp &w, double &mu_out, double &chi2_out) {
+    const Params &P = *w.P;
+    double *gam = w.scr + (long)P.m * P.n + 3L * P.K + (long)kCacheCap * 19;
+    warp_svdvals(w, gam);
+    GcvF f{&w, gam, (2.220446049250313e-16 * 2.220446049250313e-16) / P.m};
+    double logmu, logG;
+    brent_minimize(f, -8.0, 2.0, 0.0, 1e-4, 20, logmu, logG);
+    double mu = exp(logmu);
+    TikhState t = tikh_solve(w, mu);
+    double res2 = tikh_res2(w, t);
+    save_x(w);
+    double chi2 = CUDART_NAN;
+    if (P.need_chi2) {
+        NnlsResult r0 = warp_lsq(w.s, w.A, P.m, P.n, w.data, false, 0.0);
+        note(w, r0);
+        chi2 = res2 / __dmul_rn(r0.rnorm, r0.rnorm);
+    }
+    mu_out = mu;
+    chi2_out = chi2;
+}
+
+// ----------------------------------------------------------------------------
+// Flip-angle search (src/T2mapSEcorr.jl:409-423; src/splines.jl:53-110,
+// 504-566, 664-850, 975-1051)
+// ----------------------------------------------------------------------------
+struct Search {
+    Warp *w;
+    double *u, *du;       // per grid index, global scratch (K each)
+    int *sidx;            // sorted evaluated indices, 1-based (K)
+    unsigned seen[8];     // bitset over <= 256 grid points (warp-uniform registers)
+    int npts, numeval, mineval, maxeval;
+};
+__device__ __forceinline__ bool sseen(const Search &S, int I) { return (S.seen[(I - 1) >> 5] >> ((I - 1) & 31)) & 1u; }
+
+// loss_with_grad!(prob, I), src/splines.jl:1010-1041
+__device__ void fa_update(Search &S, int I) {
+    Warp &w = *S.w;
+    const Params &P = *w.P;
+    const int m = P.m, n = P.n, lane = w.lane;
+    const double *A = P.As + (long)(I - 1) * m * n, *dA = P.dAs + (long)(I - 1) * m * n;
+    NnlsResult r = warp_lsq(w.s, A, m, n, w.data, false, 0.0);
+    note(w, r);
+    double ell = __dmul_rn(r.rnorm, r.rnorm);
+    double part = 0;
+    for (int i0 = 0; i0 < m; i0 += 32) {
+        int i = i0 + lane;
+        double ax = 0, dax = 0;
+        if (i < m) {
+            for (int j = 0; j < n; ++j) {
+                double xj = w.s.x[j];
+                if (xj > 0) {
+                    ax = fma(xj, __ldg(A + i + (long)j * m), ax);
+                    dax = fma(xj, __ldg(dA + i + (long)j * m), dax);
+                }
+            }
+            part = fma(dax, ax - w.data[i], part);
+        }
+    }
+    double dt = wsum(part);
+    if (lane == 0) {
+        S.u[I - 1] = ell;
+        S.du[I - 1] = 2 * dt;
+        // insertsorted!(idx, I, npts += 1), src/utils.jl:42-49
+        int len = S.npts + 1, val = I;
+        for (int i = 0; i < len - 1; ++i) {
+            int a = S.sidx[i];
+            if (val < a) { S.sidx[i] = val; val = a; }
+        }
+        S.sidx[len - 1] = val;
+    }
+    __syncwarp();
+    S.npts++;
+}
+// update!(surr, state, I; maxeval), src/splines.jl:736-744
+__device__ bool fa_state_update(Search &S, int I) {
+    if (S.numeval >= S.maxeval) return true;
+    if (sseen(S, I)) return false;
+    fa_update(S, I);
+    S.seen[(I - 1) >> 5] |= 1u << ((I - 1) & 31);
+    S.numeval += 1;
+    return S.numeval >= S.maxeval;
+}
+__device__ __forceinline__ bool box_done(const Search &S, int lo, int hi) { return (int)sseen(S, lo) + (int)sseen(S, hi) >= 2; }
+// evaluate_box!, src/splines.jl:802-815
+__device__ void fa_evaluate_box(Search &S, int lo, int hi, bool have_x, double x) {
+    const double *g = S.w->P->angles;
+    int c0 = lo, c1 = hi;
+    if (have_x) {
+        double dlo = (g[lo - 1] - x) * (g[lo - 1] - x), dhi = (g[hi - 1] - x) * (g[hi - 1] - x);
+        if (dhi < dlo) { c0 = hi; c1 = lo; }
+    }
+    if (box_done(S, lo, hi)) return;
+    if (fa_state_update(S, c0)) return;
+    if (box_done(S, lo, hi)) return;
+    fa_state_update(S, c1);
+}
+// initialize! (recursive breadth-limited bisection), src/splines.jl:716-734,
+// run with an explicit depth-first stack.
+__device__ void fa_initialize(Search &S) {
+    const int K = S.w->P->K;
+    for (int depth = 1; depth <= S.mineval; ++depth) {
+        int st_lo[64], st_hi[64], st_d[64];
+        int sp = 0;
+        st_lo[0] = 1; st_hi[0] = K; st_d[0] = depth; sp = 1;
+        int guard = 0;
+        while (sp > 0 && guard++ < 4096) {
+            --sp;
+            int lo = st_lo[sp], hi = st_hi[sp], d = st_d[sp];
+            if (d <= 0) continue;
+            fa_evaluate_box(S, lo, hi, false, 0.0);
+            if (S.numeval >= S.mineval) continue;
+            int mid = (lo + hi) / 2;
+            if (sp + 2 > 64) { S.w->loop_caps++; break; }
+            st_lo[sp] = mid; st_hi[sp] = hi; st_d[sp] = d - 1; ++sp;  // right, processed after left
+            st_lo[sp] = lo; st_hi[sp] = mid; st_d[sp] = d - 1; ++sp;
+        }
+        if (S.numeval >= S.mineval) break;
+    }
+}
+// CubicHermiteInterpolator + minimize, src/splines.jl:62-110
+__device__ void hermite_minimize(double a, double b, double u0, double u1, double m0, double m1, double &xo, double &uo) {
+    double r = (b - a) / 2;
+    m0 = r * m0; m1 = r * m1;
+    double du = u1 - u0, dm = m1 - m0, su = u1 + u0, sm = m1 + m0;
+    double c0 = su / 2 - dm / 4, c1 = (3 * du - sm) / 4, c2 = dm / 4, c3 = (sm - du) / 4;
+    double xend, uend;
+    if (u0 < u1) { xend = a; uend = u0; } else { xend = b; uend = u1; }
+    double D = 3 * (u0 - u1), th = D / 2 + (m0 + m1);
+    double g = __dsub_rn(__dmul_rn(th, th), __dmul_rn(m0, m1));
+    g = g > 0 ? -sqrt(g) : 0.0;
+    double p = -(D + (m0 + m1)), q = 2 * g + (m0 - m1);
+    if (fabs(p) < fabs(q)) {
+        double t = p / q;
+        double y = fma(t, fma(t, fma(t, c3, c2), c1), c0);
+        if (y < uend) {
+            double cc = (a + b) / 2, rr = (b - a) / 2;
+            double xx = fma(rr, t, cc);
+            xo = xx > b ? b : (xx < a ? a : xx);
+            uo = y;
+            return;
+        }
+    }
+    xo = xend;
+    uo = uend;
+}
+// suggest_point(::CubicHermiteSplineSurrogate), src/splines.jl:544-566
+__device__ void fa_suggest(Search &S, double &xo, double &uo) {
+    const double *g = S.w->P->angles;
+    int I0 = S.sidx[0];
+    double pl = g[I0 - 1], ul = S.u[I0 - 1], dl = S.du[I0 - 1], p = pl, u = ul;
+    for (int i = 2; i <= S.npts; ++i) {
+        int I = S.sidx[i - 1];
+        double pc = g[I - 1], uc = S.u[I - 1], dc = S.du[I - 1], xx, uu;
+        hermite_minimize(pl, pc, ul, uc, dl, dc, xx, uu);
+        if (uu < u) { p = xx; u = uu; }
+        pl = pc; ul = uc; dl = dc;
+    }
+    xo = p;
+    uo = u;
+}
+// minimal_bounding_box, src/splines.jl:778-800
+__device__ void fa_min_bbox(const Search &S, double x, int &plo, int &phi) {
+    const double *g = S.w->P->angles;
+    int lo = 1, hi = S.w->P->K;
+    for (int guard = 0; guard < 64; ++guard) {
+        int mid = (lo + hi) / 2;
+        if (g[lo - 1] <= x && x <= g[mid - 1]) {
+            if (!box_done(S, lo, mid) || !(abs(mid - lo) > 1)) { plo = lo; phi = mid; return; }
+            hi = mid;
+        } else {
+            if (!box_done(S, mid, hi) || !(abs(hi - mid) > 1)) { plo = mid; phi = hi; return; }
+            lo = mid;
+        }
+    }
+    plo = lo;
+    phi = hi;
+}
+// optimize_flip_angle!, src/T2mapSEcorr.jl:409-423 + bisection_search, src/splines.jl:750-775
+__device__ double flip_angle_search(Warp &w) {
+    const Params &P = *w.P;
+    Search S;
+    S.w = &w;
+    S.u = w.scr + (long)P.m * P.n;
+    S.du = S.u + P.K;
+    S.sidx = reinterpret_cast<int *>(S.du + P.K);
+    for (int q = 0; q < 8; ++q) S.seen[q] = 0;
+    S.npts = 0; S.numeval = 0; S.mineval = P.mineval; S.maxeval = P.maxeval;
+    fa_initialize(S);
+    double x, u;
+    fa_suggest(S, x, u);
+    for (int guard = 0; guard <= kLoopCap; ++guard) {
+        int lo, hi;
+        fa_min_bbox(S, x, lo, hi);
+        fa_evaluate_box(S, lo, hi, true, x);
+        fa_suggest(S, x, u);
+        if (S.numeval >= S.maxeval || abs(hi - lo) <= 1) return x;
+    }
+    w.loop_caps++;
+    return x;
+}
+
+// ----------------------------------------------------------------------------
+// EPG basis at one angle: lanes over T2 columns, states in shared memory
+// (src/T2mapSEcorr.jl:275-283 with the default EPG kernels).
+// ----------------------------------------------------------------------------
+__device__ void warp_basis(Warp &w, double alpha, double *out /* m x n, global */) {
+    const Params &P = *w.P;
+    const int m = P.m, n = P.n, lanes = P.epg_lanes, lane = w.lane;
+    double *S = w.s.C;  // 3*m*lanes doubles, lane-contiguous
+    for (int j0 = 0; j0 < n; j0 += lanes) {
+        int j = j0 + lane;
+        if (lane < lanes && j < n) {
+            double *Sl = S + lane;
+            if (P.beta180) {
+                dx::FlatCoef<double> q = dx::flat_coef(alpha, P.TE, P.t2[j], P.T1);
+                dx::epg_flat_inplace(m, q, Sl, lanes, out + (long)j * m, 1);
+            } else {
+                dx::VecCoef<double> q = dx::vec_coef(alpha, P.TE, P.t2[j], P.T1, P.beta);
+                dx::epg_vec_inplace(m, q, Sl, lanes, out + (long)j * m, 1);
+            }
+        }
+        __syncwarp();
+    }
+    __threadfence_block();
+    __syncwarp();
+}
+
+// ----------------------------------------------------------------------------
+// One voxel (src/T2mapSEcorr.jl:201-238, save_results! 512-591, T2part 95-138)
+// ----------------------------------------------------------------------------
+__device__ void process_voxel(Warp &w, long v) {
+    const Params &P = *w.P;
+    const int m = P.m, n = P.n, lane = w.lane;
+    // copy + normalize by the maximum echo
+    double mx = 0;
+    for (int i = lane; i < m; i += 32) {
+        double bi = P.image_f32 ? (double)static_cast<const float *>(P.image)[v + P.V * i]
+                                : static_cast<const double *>(P.image)[v + P.V * i];
+        w.data[i] = bi;
+        mx = bi > mx ? bi : mx;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        double t = __shfl_xor_sync(FULL, mx, o);
+        mx = t > mx ? t : mx;
+    }
+    __syncwarp();
+    if (mx > 0)
+        for (int i = lane; i < m; i += 32) w.data[i] = w.data[i] / mx;
+    __syncwarp();
+
+    double alpha;
+    if (P.angle_mode == 1) {
+        alpha = P.fixed_angle;
+        w.A = const_cast<double *>(P.basis_fixed);
+    } else {
+        w.A = w.scr;
+        if (P.angle_mode == 2) {
+            alpha = P.image_f32 ? (double)static_cast<const float *>(P.b1map)[v] : static_cast<const double *>(P.b1map)[v];
+        } else {
+            alpha = flip_angle_search(w);
+        }
+        warp_basis(w, alpha, w.A);
+    }
+
+    double mu = CUDART_NAN, chi2 = CUDART_NAN;
+    switch (P.reg) {
+    case 0: {  // none
+        NnlsResult r = warp_lsq(w.s, w.A, m, n, w.data, false, 0.0);
+        note(w, r);
+        save_x(w);
+        mu = 0; chi2 = 1;
+        break;
+    }
+    case 1: reg_lcurve(w, mu, chi2); break;
+    case 2: reg_gcv(w, mu, chi2); break;
+    case 3: reg_chi2(w, P.chi2factor, mu, chi2); break;
+    default: {
+        double delta = sqrt((double)m) * (P.noiselevel / mx);
+        reg_mdp(w, delta, mu, chi2);
+    }
+    }
+
+    // save_results!: rescale, fit, residuals and distribution statistics
+    double sd = 0, sr2 = 0, sr = 0, dotl = 0;
+    for (int j = lane; j < n; j += 32) {
+        double dj = w.xout[j] * mx;
+        w.s.w[j] = dj;  // rescaled distribution (w is free now)
+    }
+    __syncwarp();
+    double res[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        int i = lane + 32 * t;
+        if (i < m) {
+            double fit = 0;
+            for (int j = 0; j < n; ++j) fit = fma(w.A[i + (long)j * m], w.s.w[j], fit);
+            double bi = w.data[i] * mx;
+            double ri = fit - bi;
+            res[t] = ri;
+            sr2 = __dadd_rn(sr2, __dmul_rn(ri, ri));
+            sr = __dadd_rn(sr, ri);
+            if (P.decaycurve) P.decaycurve[v + P.V * i] = fit;
+        }
+    }
+    for (int j = lane; j < n; j += 32) {
+        double dj = w.s.w[j];
+        sd = __dadd_rn(sd, dj);
+        dotl = __dadd_rn(dotl, __dmul_rn(dj, P.logt2[j]));
+    }
+    sd = wsum(sd); sr2 = wsum(sr2); sr = wsum(sr); dotl = wsum(dotl);
+    double mean = sr / m, var = 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        int i = lane + 32 * t;
+        if (i < m) { double d = res[t] - mean; var = __dadd_rn(var, __dmul_rn(d, d)); }
+    }
+    var = wsum(var);
+    double lggm = dotl / sd, lgva = 0;
+    for (int j = lane; j < n; j += 32) {
+        double d = P.logt2[j] - lggm;
+        lgva = __dadd_rn(lgva, __dmul_rn(__dmul_rn(d, d), w.s.w[j]));
+    }
+    lgva = wsum(lgva) / sd;
+    for (int j = lane; j < n; j += 32) P.dist[v + P.V * j] = w.s.w[j];
+    if (P.basis_out && P.angle_mode != 1)
+        for (long q = lane; q < (long)m * n; q += 32) P.basis_out[v + P.V * q] = w.A[q];
+    if (lane == 0) {
+        P.gdn[v] = sd;
+        P.ggm[v] = exp(lggm);
+        P.gva[v] = expm1(lgva);
+        P.fnr[v] = sd / sqrt(sr2 / (m - 1));
+        P.snr[v] = mx / sqrt(var / (m - 1));
+        P.alpha[v] = alpha;
+        if (P.resnorm) P.resnorm[v] = sqrt(sr2);
+        if (P.mu) P.mu[v] = mu;
+        if (P.chi2f) P.chi2f[v] = chi2;
+    }
+    // fused T2partSEcorr window sums (src/T2partSEcorr.jl:95-138)
+    if (P.fuse_t2part) {
+        double tsd = 0, ssp = 0, smp = 0, dsp = 0, dmp = 0, dw = 0;
+        bool anynan = false;
+        for (int j = lane; j < n; j += 32) {
+            double d = w.s.w[j];
+            anynan |= isnan(d);
+            tsd = __dadd_rn(tsd, d);
+            if (j >= P.sp0 && j <= P.sp1) { dsp = __dadd_rn(dsp, __dmul_rn(d, P.logt2[j])); ssp = __dadd_rn(ssp, d); }
+            if (j >= P.mp0 && j <= P.mp1) { dmp = __dadd_rn(dmp, __dmul_rn(d, P.logt2[j])); smp = __dadd_rn(smp, d); }
+            if (P.weights) dw = __dadd_rn(dw, __dmul_rn(d, P.weights[j]));
+        }
+        anynan = __any_sync(FULL, anynan);
+        tsd = wsum(tsd); ssp = wsum(ssp); smp = wsum(smp); dsp = wsum(dsp); dmp = wsum(dmp); dw = wsum(dw);
+        if (lane == 0 && !anynan) {
+            if (tsd > 0) {
+                P.sfr[v] = P.weights ? dw / tsd : ssp / tsd;
+                P.mfr[v] = smp / tsd;
+            }
+            if (ssp > 0) P.sgm[v] = exp(dsp / ssp);
+            if (smp > 0) P.mgm[v] = exp(dmp / smp);
+        }
+    }
+    __syncwarp();
+}
+
+}  // namespace dk

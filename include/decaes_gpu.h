@@ -1,0 +1,184 @@
+/*
+ * decaes_gpu.h -- C ABI of libdecaes_gpu.so, the GB300 (sm_103a) implementation
+ * of DECAES.jl's voxelwise T2-distribution path.
+ *
+ * The entry points are what the reference's Julia API would `ccall` for the
+ * path: plain pointers and sizes, caller-owned buffers, column-major (Julia)
+ * array layout, no Julia or torch types.  All outputs are caller-allocated and
+ * NaN-prefilled by the caller as the reference's T2Maps/T2Distributions/T2Parts
+ * constructors do; the library writes only processed voxels.
+ *
+ * Layouts (V = MatrixSize[0]*MatrixSize[1]*MatrixSize[2]):
+ *   image        V x nTE     (image[v + V*e]),  DECAES_F32 or DECAES_F64
+ *   dist         V x nT2
+ *   maps         V
+ *   decaycurve   V x nTE
+ *   decaybasis   V x nTE x nT2 (or nTE x nT2 when SetFlipAngle is given)
+ *
+ * Errors: every entry point returns 0 on success and a nonzero DECAES_E* code
+ * otherwise; decaes_last_error() returns the message.  Option errors carry the
+ * reference's assertion text (src/types.jl).
+ */
+#ifndef DECAES_GPU_H
+#define DECAES_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { DECAES_F32 = 0, DECAES_F64 = 1 };
+enum { DECAES_REG_NONE = 0, DECAES_REG_LCURVE = 1, DECAES_REG_GCV = 2, DECAES_REG_CHI2 = 3, DECAES_REG_MDP = 4 };
+/* Arithmetic of the path.  FP64: every step in IEEE binary64 (the plain method).
+ * MIXED: EPG recursion and least-squares solves on the FP32 pipes with error
+ * compensation where the basis is ill-conditioned; root finding, curvature and
+ * the spline fit stay FP64. */
+enum { DECAES_PREC_FP64 = 0, DECAES_PREC_MIXED = 1 };
+enum {
+    DECAES_OK = 0,
+    DECAES_EINVAL = 1,   /* invalid option or argument (reference AssertionError) */
+    DECAES_ECUDA = 2,    /* CUDA runtime error */
+    DECAES_ENOMEM = 3,   /* allocation would exceed the context's HBM budget */
+    DECAES_ELEGACY = 4,  /* legacy=true algorithms are not provided */
+};
+
+typedef struct decaes_ctx decaes_ctx;
+
+/* Mirrors T2mapOptions{T} (src/types.jl:19-100).  Optional reference fields
+ * (`Union{T,Nothing}`) use NaN for `nothing`. */
+typedef struct {
+    int32_t MatrixSize[3];
+    int32_t nTE;
+    double TE;
+    int32_t nT2;
+    double T2Range[2];
+    double T1;
+    double Threshold;
+    double MinRefAngle;
+    int32_t nRefAngles;
+    int32_t nRefAnglesMin;
+    int32_t Reg;          /* DECAES_REG_* */
+    double Chi2Factor;    /* NaN = nothing */
+    double NoiseLevel;    /* NaN = nothing */
+    double RefConAngle;
+    double SetFlipAngle;  /* NaN = nothing */
+    int32_t SaveResidualNorm;
+    int32_t SaveDecayCurve;
+    int32_t SaveRegParam;
+    int32_t SaveNNLSBasis;
+    int32_t legacy;       /* must be 0 */
+    int32_t precision;    /* DECAES_PREC_* (extension; not a reference field) */
+} decaes_t2map_opts;
+
+/* Output buffers of T2mapSEcorr (src/T2mapSEcorr.jl:2-19, 64-72), all of the
+ * call's dtype.  NULL skips an optional output. */
+typedef struct {
+    void *dist;
+    void *gdn, *ggm, *gva, *fnr, *snr, *alpha;
+    void *resnorm, *decaycurve, *mu, *chi2factor, *decaybasis;
+    /* per-call constants: echotimes (nTE), t2times (nT2), refangleset
+     * (nRefAngles, or 1 with SetFlipAngle), decaybasisset (nTE x nT2 x nRefAngles,
+     * or nTE x nT2 with SetFlipAngle) */
+    void *echotimes, *t2times, *refangleset, *decaybasisset;
+} decaes_t2map_out;
+
+/* Mirrors T2partOptions{T} (src/types.jl:139-172). */
+typedef struct {
+    int32_t MatrixSize[3];
+    int32_t nT2;
+    double T2Range[2];
+    double SPWin[2];
+    double MPWin[2];
+    double Sigmoid; /* NaN = nothing */
+    int32_t legacy; /* must be 0 */
+} decaes_t2part_opts;
+
+typedef struct {
+    void *sfr, *sgm, *mfr, *mgm;
+} decaes_t2part_out;
+
+/* Per-call statistics of the most recent call on a context. */
+typedef struct {
+    int64_t voxels;            /* prod(MatrixSize) */
+    int64_t voxels_processed;  /* above Threshold */
+    int64_t nnls_cap_hits;     /* NNLS solves that reached max_iter = 3n (reference mode = 1) */
+    int64_t search_limit_hits; /* flip-angle / L-curve loops stopped by their device iteration caps */
+    double ms_total;           /* device time of the whole call (CUDA events, incl. copies) */
+    double ms_solve;           /* device time of the voxel-solve kernel */
+    double ms_h2d, ms_d2h;     /* device time of the host<->device copies */
+    int32_t solve_launches;    /* voxel-solve kernel launches of the call */
+    int32_t kernel_launches;   /* all kernels launched by the call */
+} decaes_stats;
+
+/* ---- context -------------------------------------------------------------
+ * One context per device; it owns device buffers, the stream and resident
+ * per-parameter bases.  hbm_budget_bytes = 0 means 160 GiB.  Calls on one
+ * context are serialized. */
+decaes_ctx *decaes_create(int device, size_t hbm_budget_bytes);
+void decaes_destroy(decaes_ctx *ctx);
+const char *decaes_last_error(const decaes_ctx *ctx);
+int decaes_get_stats(const decaes_ctx *ctx, decaes_stats *out);
+
+/* Option validation with the reference's assertion messages; needs no GPU.
+ * Replaces the @assert blocks of T2mapOptions (src/types.jl:28-95) and
+ * T2partOptions (src/types.jl:148-168). */
+int decaes_t2map_check_options(const decaes_t2map_opts *opts, char *msg, size_t msglen);
+int decaes_t2part_check_options(const decaes_t2part_opts *opts, char *msg, size_t msglen);
+
+/* T2mapSEcorr!(maps, dist, image, opts) (src/T2mapSEcorr.jl:151-196).
+ * Host buffers.  b1map (V values of the call dtype) replaces the flip-angle
+ * search by the given angles, as load_B1map! does (src/T2mapSEcorr.jl:56-61).
+ * The plain method computes in FP64 whatever the dtype (FP32 input is widened
+ * on the device, as the reference CLI does in src/main.jl:612-617). */
+int decaes_t2map(decaes_ctx *ctx, const decaes_t2map_opts *opts, const void *image, int dtype,
+                 const void *b1map, decaes_t2map_out *out);
+
+/* T2partSEcorr(dist, opts) (src/T2partSEcorr.jl:42-71).  Host buffers. */
+int decaes_t2part(decaes_ctx *ctx, const decaes_t2part_opts *opts, const void *dist, int dtype,
+                  decaes_t2part_out *out);
+
+/* T2mapSEcorr followed by T2partSEcorr on its distribution, with the T2part
+ * window sums fused into the voxel-solve epilogue.  Host buffers. */
+int decaes_t2map_t2part(decaes_ctx *ctx, const decaes_t2map_opts *mopts, const decaes_t2part_opts *popts,
+                        const void *image, int dtype, const void *b1map, decaes_t2map_out *mout,
+                        decaes_t2part_out *pout);
+
+/* Device-pointer variants: all pointers are device addresses on the context's
+ * device; `stream` is a cudaStream_t (NULL = the context's stream).  Used for
+ * in-HBM throughput measurement and by callers that keep data resident. */
+int decaes_t2map_t2part_device(decaes_ctx *ctx, const decaes_t2map_opts *mopts, const decaes_t2part_opts *popts,
+                               const void *d_image, int dtype, const void *d_b1map, decaes_t2map_out *d_mout,
+                               decaes_t2part_out *d_pout, void *stream);
+/* Waits for the last device-pointer call on `stream` and completes its
+ * decaes_stats (processed voxels, cap hits, device times). */
+int decaes_sync_stats(decaes_ctx *ctx, void *stream);
+
+/* Synthetic multi-echo image, the counterpart of mock_image
+ * (src/utils.jl:606-668) with the generator used by this project's benchmarks:
+ * per voxel a sum of three EPG decays (myelin, intra/extracellular, CSF) with
+ * Rician noise.  Host function (no GPU); deterministic for a given seed and
+ * independent of thread count. */
+typedef struct {
+    int32_t MatrixSize[3];
+    int32_t nTE;
+    double TE;
+    double T1;
+    double FlipAngleRange[2];   /* degrees, uniform */
+    double MyelinT2Range[2];    /* seconds */
+    double MyelinFracRange[2];
+    double IET2Range[2];
+    double CSFT2Range[2];
+    double CSFFracRange[2];
+    double AmplitudeRange[2];
+    double SNRRange[2];         /* linear SNR; noise sigma = amplitude / SNR */
+    double BackgroundFraction;  /* voxels with zero amplitude (noise only) */
+    double BackgroundSigma;     /* noise sigma of background voxels */
+} decaes_mock_opts;
+int decaes_mock_image(const decaes_mock_opts *opts, uint64_t seed, void *image, int dtype, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
