@@ -1,0 +1,326 @@
+#!/usr/bin/env python
+"""Throughput of the voxelwise T2mapSEcorr + T2partSEcorr path on GB300.
+
+Workload (the 48-echo configuration of the reference's headline table):
+240x240x48 voxels, 48 echoes, TE = 10 ms, nT2 = 40 over 10 ms - 2 s,
+nRefAngles = 32 with the spline flip-angle search, Reg = "lcurve", Float32
+input; T2part windows SPWin 10-25 ms, MPWin 25-200 ms.  Synthetic, seeded:
+three EPG compartments + Rician noise, 35% background voxels excluded by the
+threshold.  A step is one pass of T2map+T2part over the whole volume.
+
+  value  voxels/s with the image resident in HBM (device-pointer C ABI call)
+  e2e    the same metric through the host-buffer C ABI call from pinned
+         memory (H2D of the image and D2H of all outputs inside the timing)
+  --impl reference  times the CPU restatement of the reference path (the
+         oracle, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "decaes.jl_gb300"))
+
+METRIC = "voxels/s T2map+T2part, 240×240×48×48 echoes: FP64 vs mixed prec @MWF|Δ|≤1e-3; p99"
+SPWIN, MPWIN = (10e-3, 25e-3), (25e-3, 200e-3)
+THRESHOLD = 200.0
+
+
+def workload(matrix, precision):
+    import decaes_gb300 as D
+    mo = D.T2mapOptions(MatrixSize=matrix, nTE=48, TE=10e-3, nT2=40, T2Range=(10e-3, 2.0), Reg="lcurve",
+                        nRefAngles=32, MinRefAngle=50.0, Threshold=THRESHOLD, precision=precision)
+    po = D.T2partOptions.from_t2map(mo, SPWin=SPWIN, MPWin=MPWIN)
+    mock = D.MockImageOptions(MatrixSize=matrix, nTE=48, TE=10e-3, BackgroundFraction=0.35)
+    return mo, po, mock
+
+
+def config_dict(matrix, precision, V, Vp):
+    return {
+        "workload": f"{matrix[0]}x{matrix[1]}x{matrix[2]} voxels x 48 echoes, TE=10ms, nT2=40 (10ms-2s), "
+                    f"nRefAngles=32 (spline flip-angle search), Reg=lcurve, Float32 input, "
+                    f"T2part SPWin 10-25ms MPWin 25-200ms",
+        "precision": precision,
+        "voxels": V,
+        "voxels_above_threshold": Vp,
+        "l2": "inputs larger than L2 (530 MB image vs 129 MB L2); no flush needed",
+        "parallelism": "replicas (independent volume per GPU)",
+    }
+
+
+class Clocks:
+    """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = [r for r in self.rows if len(r) >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[4 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def fp64_peak_tflops(torch):
+    """cuBLAS DGEMM throughput on this GPU (the FP64 roofline denominator)."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 1e30
+    for _ in range(5):
+        e0.record()
+        a @ b
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def cpu_baseline(mo, img_f32, sample, threads):
+    """The oracle (CPU restatement of the reference path) on a bounded sample of
+    above-threshold voxels; returns (voxels/s scaled to the whole image,
+    seconds, FP64 FLOPs per processed voxel)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    V = int(np.prod(mo.MatrixSize))
+    flat = img_f32.reshape((V, mo.nTE), order="F")
+    fg = np.flatnonzero(flat[:, 0] > mo.Threshold)
+    pick = fg[np.linspace(0, len(fg) - 1, min(sample, len(fg))).astype(np.int64)]
+    sub = flat[pick].astype(np.float64).reshape((len(pick), 1, 1, mo.nTE), order="F")
+    oo = O.T2mapOptions(MatrixSize=(len(pick), 1, 1), nTE=mo.nTE, TE=mo.TE, nT2=mo.nT2, T2Range=mo.T2Range,
+                        Reg=mo.Reg, nRefAngles=mo.nRefAngles, MinRefAngle=mo.MinRefAngle, Threshold=mo.Threshold,
+                        nRefAnglesMin=mo.nRefAnglesMin)
+    t0 = time.perf_counter()
+    maps, dist, fl = O.t2map(sub, oo, nthreads=threads, return_flops=True)
+    O.t2part(dist, O.T2partOptions(MatrixSize=(len(pick), 1, 1), nT2=mo.nT2, T2Range=mo.T2Range, SPWin=SPWIN,
+                                   MPWin=MPWIN))
+    dt = time.perf_counter() - t0
+    per_fg = dt / len(pick)
+    whole = per_fg * len(fg)  # projected time for the whole volume
+    return V / whole, dt, sum(fl.values()) / len(pick), len(pick), len(fg)
+
+
+def traffic_per_voxel():
+    """DRAM bytes per processed voxel of the voxel-solve kernel from the
+    committed ncu summary (None when absent)."""
+    p = os.path.join(ROOT, "profiles", "k_voxels_lcurve48.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_voxel:"):
+            return float(line.split(":")[1])
+    return None
+
+
+def run_reference(args):
+    """Times the oracle (CPU restatement of the reference path) on host cores."""
+    import decaes_gb300 as D
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    matrix = tuple(args.matrix)
+    mo, po, mock = workload(matrix, "fp64")
+    img = D.mock_image(mock, seed=args.seed, dtype=np.float32)
+    threads = os.cpu_count() or 1
+    sample = args.cpu_sample
+    for _ in range(args.warmup):
+        cpu_baseline(mo, img, max(64, sample // 16), threads)
+    vals = []
+    for _ in range(args.steps):
+        v, dt, flv, ns, nfg = cpu_baseline(mo, img, sample, threads)
+        vals.append(v)
+    V = int(np.prod(matrix))
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": V / value * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded 3-compartment EPG + Rician noise, 35% background)",
+        "config": config_dict(matrix, "fp64", V, nfg),
+        "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": threads, "kind": "port",
+                         "sample": f"{ns} above-threshold voxels per step (of {nfg}); time scaled to the whole volume"},
+        "e2e": {"value": value, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--matrix", type=int, nargs=3, default=[240, 240, 48])
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--cpu-sample", type=int, default=2048)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import decaes_gb300 as D
+    from decaes_gb300 import _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    matrix = tuple(args.matrix)
+    V = int(np.prod(matrix))
+    mo, po, mock = workload(matrix, args.precision)
+    img = D.mock_image(mock, seed=args.seed + rank, dtype=np.float32)
+    ctx = D.Context(local)
+    L = ctx.L
+
+    # ---- device-resident inputs and outputs (torch owns the memory) ----
+    stream = torch.cuda.current_stream()
+    d_img = torch.from_numpy(img.reshape(-1, order="F").copy()).cuda()
+    n, m = mo.nT2, mo.nTE
+    keys = ["dist", "gdn", "ggm", "gva", "fnr", "snr", "alpha"]
+    d_out = {"dist": torch.empty(V * n, dtype=torch.float32, device="cuda")}
+    for k in keys[1:]:
+        d_out[k] = torch.empty(V, dtype=torch.float32, device="cuda")
+    d_parts = {k: torch.empty(V, dtype=torch.float32, device="cuda") for k in ("sfr", "sgm", "mfr", "mgm")}
+    mout = _lib.T2mapOutC(*[C.c_void_p(d_out[k].data_ptr()) if k in d_out else None for k, _ in _lib.T2mapOutC._fields_])
+    pout = _lib.T2partOutC(*[C.c_void_p(d_parts[k].data_ptr()) for k, _ in _lib.T2partOutC._fields_])
+    mo_c, po_c = mo.to_c(), po.to_c()
+
+    def device_step():
+        ctx.check(L.decaes_t2map_t2part_device(ctx.h, C.byref(mo_c), C.byref(po_c), C.c_void_p(d_img.data_ptr()),
+                                               _lib.F32, None, C.byref(mout), C.byref(pout),
+                                               C.c_void_p(stream.cuda_stream)))
+
+    for _ in range(args.warmup):
+        device_step()
+    torch.cuda.synchronize()
+    ctx.check(L.decaes_sync_stats(ctx.h, C.c_void_p(stream.cuda_stream)))
+    Vp = ctx.stats()["voxels_processed"]
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    solve_ms, launches = [], 0
+    with Clocks(local) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            device_step()
+            ctx.check(L.decaes_sync_stats(ctx.h, C.c_void_p(stream.cuda_stream)))
+            st = ctx.stats()
+            solve_ms.append(st["ms_solve"])
+            launches += st["kernel_launches"]
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    ms_per_step = ms / args.steps
+    value = world * V * args.steps / (ms * 1e-3)
+
+    # ---- end to end through the host-buffer C ABI from pinned memory ----
+    h_img = torch.from_numpy(img.reshape(-1, order="F").copy()).pin_memory()
+    h_out = {k: torch.empty_like(v, device="cpu").pin_memory() for k, v in d_out.items()}
+    h_parts = {k: torch.empty_like(v, device="cpu").pin_memory() for k, v in d_parts.items()}
+    hm = _lib.T2mapOutC(*[C.c_void_p(h_out[k].data_ptr()) if k in h_out else None for k, _ in _lib.T2mapOutC._fields_])
+    hp = _lib.T2partOutC(*[C.c_void_p(h_parts[k].data_ptr()) for k, _ in _lib.T2partOutC._fields_])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.check(L.decaes_t2map_t2part(ctx.h, C.byref(mo_c), C.byref(po_c), C.c_void_p(h_img.data_ptr()), _lib.F32,
+                                        None, C.byref(hm), C.byref(hp)))
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    h2d = img.nbytes
+    d2h = sum(v.numel() * 4 for v in h_out.values()) + sum(v.numel() * 4 for v in h_parts.values())
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
+        "data": "synthetic (seeded 3-compartment EPG + Rician noise, 35% background)",
+        "config": config_dict(matrix, args.precision, V, Vp),
+        "e2e": {"value": world * V / e2e_s, "unit": "voxels/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    # ---- roofline of the voxel-solve kernel and the CPU baseline ----
+    peak = fp64_peak_tflops(torch)
+    if not args.no_cpu_baseline:
+        cv, cdt, flops_per_voxel, ns, nfg = cpu_baseline(mo, img, args.cpu_sample, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": cv, "unit": "voxels/s", "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": f"{ns} above-threshold voxels of the same image ({cdt:.1f} s); "
+                                          f"time scaled to the whole volume"}
+        kern_ms = statistics.median(solve_ms)
+        achieved = flops_per_voxel * Vp / (kern_ms * 1e-3) / 1e12
+        tpv = traffic_per_voxel()
+        line["roofline"] = {"kernel": "k_voxels", "bound": "fp64", "achieved": achieved, "peak": peak,
+                            "unit": "TFLOP/s", "frac": achieved / peak,
+                            "traffic": None if tpv is None else tpv * Vp,
+                            "work": f"{flops_per_voxel / 1e6:.3f} MFLOP FP64 per above-threshold voxel "
+                                    f"(oracle-counted) x {Vp} voxels",
+                            "kernel_ms": kern_ms,
+                            "peak_source": "cuBLAS DGEMM (torch.matmul float64 4096^3) measured in this run"}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

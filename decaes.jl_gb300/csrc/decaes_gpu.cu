@@ -151,8 +151,8 @@ __global__ void k_t2part(const T *dist, long V, int n, int sp0, int sp1, int mp0
             }
             mfr[v] = smp / sd;
         }
-        if (ssp > 0) sgm[v] = exp(dsp / ssp);
-        if (smp > 0) mgm[v] = exp(dmp / smp);
+        if (ssp > 0) sgm[v] = pm_exp(dsp / ssp);
+        if (smp > 0) mgm[v] = pm_exp(dmp / smp);
     }
 }
 

@@ -16,6 +16,8 @@
 #pragma once
 #include <cmath>
 
+#include "pmath.h"
+
 #ifdef __CUDACC__
 #define DX_HD __host__ __device__ __forceinline__
 #else
@@ -63,12 +65,14 @@ DX_HD Dual zero_of(Dual) { return Dual{0.0, 0.0}; }
 // sind: the degree reduction of Base.sind with a double-double radian
 // argument (sin(h + l) = sin h + l cos h to first order).
 DX_HD double sin_dd(double y) {
-    double h = y * kD2R, l = fma(y, kD2R, -h) + y * kD2RLo;
-    return sin(h) + l * cos(h);
+    double h = y * kD2R, l = fma(y, kD2R, -h) + y * kD2RLo, sh, ch;
+    pm_sincos(h, &sh, &ch);
+    return sh + l * ch;
 }
 DX_HD double cos_dd(double y) {
-    double h = y * kD2R, l = fma(y, kD2R, -h) + y * kD2RLo;
-    return cos(h) - l * sin(h);
+    double h = y * kD2R, l = fma(y, kD2R, -h) + y * kD2RLo, sh, ch;
+    pm_sincos(h, &sh, &ch);
+    return ch - l * sh;
 }
 DX_HD double sgn(double x) { return x < 0 ? -1.0 : (x > 0 ? 1.0 : x); }
 DX_HD double sind(double x) {
@@ -90,8 +94,9 @@ struct FlatCoef {
 };
 DX_HD FlatCoef<double> flat_coef(double alpha_deg, double TE, double T2, double T1) {
     double al = alpha_deg * kD2R;
-    double E1 = exp(-(TE / 2) / T1), E2 = exp(-(TE / 2) / T2);
-    double sa = sin(al), ca = cos(al);
+    double E1 = pm_exp(-(TE / 2) / T1), E2 = pm_exp(-(TE / 2) / T2);
+    double sa, ca;
+    pm_sincos(al, &sa, &ca);
     double E22h = (E2 * E2) / 2, E1E2 = E1 * E2, E11 = E1 * E1;
     FlatCoef<double> k;
     k.a = E22h;
@@ -104,8 +109,9 @@ DX_HD FlatCoef<double> flat_coef(double alpha_deg, double TE, double T2, double 
 }
 DX_HD FlatCoef<Dual> flat_coef_dual(double alpha_deg, double TE, double T2, double T1) {
     Dual al{alpha_deg * kD2R, kD2R};
-    double E1 = exp(-(TE / 2) / T1), E2 = exp(-(TE / 2) / T2);
-    double s = sin(al.v), co = cos(al.v);
+    double E1 = pm_exp(-(TE / 2) / T1), E2 = pm_exp(-(TE / 2) / T2);
+    double s, co;
+    pm_sincos(al.v, &s, &co);
     Dual sa{s, co * al.d}, ca{co, -s * al.d};
     double E22h = (E2 * E2) / 2, E1E2 = E1 * E2, E11 = E1 * E1;
     FlatCoef<Dual> k;
@@ -114,7 +120,7 @@ DX_HD FlatCoef<Dual> flat_coef_dual(double alpha_deg, double TE, double T2, doub
     k.c = sa * E1E2;
     k.d = ca * E11;
     k.cp = (-k.c) / 2;
-    k.m0 = Dual{sind(alpha_deg / 2), kD2R * cos((alpha_deg / 2) * kD2R) * 0.5};
+    k.m0 = Dual{sind(alpha_deg / 2), kD2R * pm_cos((alpha_deg / 2) * kD2R) * 0.5};
     return k;
 }
 
@@ -186,10 +192,11 @@ DX_HD T dot3(const T *a, T x, T y, T z) {
 DX_HD VecCoef<double> vec_coef(double alpha_deg, double TE, double T2, double T1, double beta) {
     double A = alpha_deg / 180;
     double a1r = (A * 180) * kD2R, air = (A * beta) * kD2R;
-    double E1 = exp(-(TE / 2) / T1), E2 = exp(-(TE / 2) / T2);
-    double sh = sin(a1r / 2), ch = cos(a1r / 2);
+    double E1 = pm_exp(-(TE / 2) / T1), E2 = pm_exp(-(TE / 2) / T2);
+    double sh, ch, sai, cai;
+    pm_sincos(a1r / 2, &sh, &ch);
+    pm_sincos(air, &sai, &cai);
     double sh2 = sh * sh, ch2 = ch * ch, sa1 = 2 * sh * ch;
-    double sai = sin(air), cai = cos(air);
     double chi2 = (1 + cai) / 2, shi2 = 1 - chi2;
     VecCoef<double> k;
     k.a1 = (E2 * E2) * ch2; k.b1 = (E2 * E2) * sh2; k.c1 = (E1 * E2) * sa1;
@@ -204,11 +211,14 @@ DX_HD VecCoef<Dual> vec_coef_dual(double alpha_deg, double TE, double T2, double
     Dual alpha{alpha_deg, 1.0};
     Dual A = alpha / 180;
     Dual a1r = (A * 180.0) * kD2R, air = (A * beta) * kD2R;
-    double E1 = exp(-(TE / 2) / T1), E2 = exp(-(TE / 2) / T2);
+    double E1 = pm_exp(-(TE / 2) / T1), E2 = pm_exp(-(TE / 2) / T2);
     Dual h = a1r / 2;
-    Dual sh{sin(h.v), cos(h.v) * h.d}, ch{cos(h.v), -sin(h.v) * h.d};
+    double shv, chv, saiv, caiv;
+    pm_sincos(h.v, &shv, &chv);
+    pm_sincos(air.v, &saiv, &caiv);
+    Dual sh{shv, chv * h.d}, ch{chv, -shv * h.d};
     Dual sh2 = sh * sh, ch2 = ch * ch, sa1 = (sh * 2.0) * ch;
-    Dual sai{sin(air.v), cos(air.v) * air.d}, cai{cos(air.v), -sin(air.v) * air.d};
+    Dual sai{saiv, caiv * air.d}, cai{caiv, -saiv * air.d};
     Dual chi2 = (mkd(1.0) + cai) / 2, shi2 = mkd(1.0) - chi2;
     VecCoef<Dual> k;
     k.a1 = ch2 * (E2 * E2); k.b1 = sh2 * (E2 * E2); k.c1 = sa1 * (E1 * E2);

@@ -218,7 +218,7 @@ struct Chi2F {  // f(logμ) of lsqnonneg_chi2!, src/lsqnonneg.jl:566-569
     Warp *w;
     double target;
     __device__ double operator()(double logmu) {
-        TikhState t = tikh_solve(*w, exp(logmu));
+        TikhState t = tikh_solve(*w, pm_exp(logmu));
         return (tikh_res2(*w, t) - target) / target;
     }
 };
@@ -226,7 +226,7 @@ struct MdpF {  // f(logμ) of lsqnonneg_mdp!, src/lsqnonneg.jl:723-726
     Warp *w;
     double delta2;
     __device__ double operator()(double logmu) {
-        TikhState t = tikh_solve(*w, exp(logmu));
+        TikhState t = tikh_solve(*w, pm_exp(logmu));
         return tikh_res2(*w, t) - delta2;
     }
 };
@@ -257,7 +257,7 @@ __device__ void reg_chi2(Warp &w, double chi2_target, double &mu_out, double &ch
     }
     double mu, res2;
     if (isfinite(relerr)) {
-        mu = exp(logmu);
+        mu = pm_exp(logmu);
         res2 = f.target * (1 + relerr);
         tikh_solve(w, mu);
     } else {
@@ -298,7 +298,7 @@ __device__ void reg_mdp(Warp &w, double delta, double &mu_out, double &chi2_out)
     }
     double mu, res2;
     if (isfinite(err)) {
-        mu = exp(logmu);
+        mu = pm_exp(logmu);
         res2 = delta * delta + err;
         tikh_solve(w, mu);
     } else {
@@ -334,11 +334,11 @@ __device__ void lc_eval(LCurve &L, double x, double &P0, double &P1) {
     for (int i = 0; i < L.flen; ++i)
         if (isapprox(x, L.fx[i])) { P0 = L.fP[2 * i]; P1 = L.fP[2 * i + 1]; return; }
     Warp &w = *L.w;
-    TikhState t = tikh_solve(w, exp(x));
+    TikhState t = tikh_solve(w, pm_exp(x));
     double res2 = tikh_res2(w, t);
     double ssq = warp_seminorm_sq(w.s, t.r.nsetp);
-    P0 = log(res2);
-    P1 = log(ssq);
+    P0 = pm_log(res2);
+    P1 = pm_log(ssq);
     if (L.flen < kCacheCap) {
         if (w.lane == 0) { L.fx[L.flen] = x; L.fP[2 * L.flen] = P0; L.fP[2 * L.flen + 1] = P1; }
         __syncwarp();
@@ -462,7 +462,7 @@ __device__ void reg_lcurve(Warp &w, double &mu_out, double &chi2_out) {
     L.px = L.fP + 2 * kCacheCap; L.pP = L.px + kCacheCap; L.pC = L.pP + 2 * kCacheCap;
     L.sx = L.pC + kCacheCap; L.sP = L.sx + 4 * kCacheCap;
     double logmu = lcurve_corner(L, -8.0, 2.0, 1e-4, 1e-4, 1e-4);
-    double mu = exp(logmu);
+    double mu = pm_exp(logmu);
     TikhState t = tikh_solve(w, mu);
     double res2 = tikh_res2(w, t);
     save_x(w);
@@ -540,14 +540,14 @@ struct GcvF {  // log𝒢(logμ), src/lsqnonneg.jl:1150-1154 and gcv!, 1213-1229
     double low;
     __device__ double operator()(double logmu) {
         const Params &P = *w->P;
-        double mu = exp(logmu);
+        double mu = pm_exp(logmu);
         TikhState t = tikh_solve(*w, mu);
         double res2 = tikh_res2(*w, t);
         int k = P.m < P.n ? P.m : P.n;
         double dof = (double)(P.m - P.n > 0 ? P.m - P.n : 0), l2 = mu * mu;
         for (int i = 0; i < k; ++i) { double g2 = gam[i] * gam[i]; dof += l2 / (g2 + l2); }
         double G = res2 / (dof * dof);
-        return log(jmax(G, low));
+        return pm_log(jmax(G, low));
     }
 };
 __device__ void reg_gcv(Warp &w, double &mu_out, double &chi2_out) {
@@ -557,7 +557,7 @@ __device__ void reg_gcv(Warp &w, double &mu_out, double &chi2_out) {
     GcvF f{&w, gam, (2.220446049250313e-16 * 2.220446049250313e-16) / P.m};
     double logmu, logG;
     brent_minimize(f, -8.0, 2.0, 0.0, 1e-4, 20, logmu, logG);
-    double mu = exp(logmu);
+    double mu = pm_exp(logmu);
     TikhState t = tikh_solve(w, mu);
     double res2 = tikh_res2(w, t);
     save_x(w);
@@ -879,8 +879,8 @@ __device__ void process_voxel(Warp &w, long v) {
         for (long q = lane; q < (long)m * n; q += 32) P.basis_out[v + P.V * q] = w.A[q];
     if (lane == 0) {
         P.gdn[v] = sd;
-        P.ggm[v] = exp(lggm);
-        P.gva[v] = expm1(lgva);
+        P.ggm[v] = pm_exp(lggm);
+        P.gva[v] = pm_expm1(lgva);
         P.fnr[v] = sd / sqrt(sr2 / (m - 1));
         P.snr[v] = mx / sqrt(var / (m - 1));
         P.alpha[v] = alpha;
@@ -907,8 +907,8 @@ __device__ void process_voxel(Warp &w, long v) {
                 P.sfr[v] = P.weights ? dw / tsd : ssp / tsd;
                 P.mfr[v] = smp / tsd;
             }
-            if (ssp > 0) P.sgm[v] = exp(dsp / ssp);
-            if (smp > 0) P.mgm[v] = exp(dmp / smp);
+            if (ssp > 0) P.sgm[v] = pm_exp(dsp / ssp);
+            if (smp > 0) P.mgm[v] = pm_exp(dmp / smp);
         }
     }
     __syncwarp();

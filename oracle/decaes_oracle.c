@@ -19,6 +19,7 @@
  *     reference.
  */
 #include "decaes_oracle.h"
+#include "orc_pmath.h"
 
 #include <complex.h>
 #undef I /* the grid index below is named I, as in the reference */
@@ -35,6 +36,21 @@
 static __thread double g_fl[ORC_NSTAGES];
 static __thread int g_st;
 #define FL(k) (g_fl[g_st] += (double)(k))
+
+/* The GPU path reduces across a 32-lane warp: element i of a loop starting at
+ * `start` accumulates into lane (i - start) mod 32, then a butterfly adds
+ * lane partials (p[l] + p[l^16], then ^8, ^4, ^2, ^1).  Julia's @simd permits
+ * exactly this kind of reassociation; the oracle uses the same order so the
+ * two agree bit for bit. */
+typedef struct { double p[32]; } lacc;
+static inline double lacc_tree(lacc *L) {
+    double t[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int l = 0; l < 32; ++l) t[l] = L->p[l] + L->p[l ^ o];
+        memcpy(L->p, t, sizeof t);
+    }
+    return L->p[0];
+}
 
 /* ------------------------------------------------------------------------- */
 /* Julia scalar semantics                                                     */
@@ -185,12 +201,14 @@ void orc_logrange(double a, double b, int len, double *out) {
  * double-double radian argument (sin(h + l) ~ sin h + l cos h). */
 static const double D2R_LO = 2.9486522708701687e-19; /* pi/180 - D2R */
 static double sin_dd(double y) {
-    double h = y * D2R, l = fma(y, D2R, -h) + y * D2R_LO;
-    return sin(h) + l * cos(h);
+    double h = y * D2R, l = fma(y, D2R, -h) + y * D2R_LO, sh, ch;
+    pm_sincos(h, &sh, &ch);
+    return sh + l * ch;
 }
 static double cos_dd(double y) {
-    double h = y * D2R, l = fma(y, D2R, -h) + y * D2R_LO;
-    return cos(h) - l * sin(h);
+    double h = y * D2R, l = fma(y, D2R, -h) + y * D2R_LO, sh, ch;
+    pm_sincos(h, &sh, &ch);
+    return ch - l * sh;
 }
 double orc_sind(double x) {
     if (isnan(x) || isinf(x)) return NAN;
@@ -242,8 +260,9 @@ static void epg_flat(int ETL, double alpha_deg, double TE, double T2, double T1,
     double *M1 = work, *M2 = work + 3 * ETL, *t;
     memset(work, 0, sizeof(double) * 6 * ETL);
     double al = alpha_deg * D2R;
-    double E1 = exp(-(TE / 2) / T1), E2 = exp(-(TE / 2) / T2);
-    double sa = sin(al), ca = cos(al);
+    double E1 = pm_exp(-(TE / 2) / T1), E2 = pm_exp(-(TE / 2) / T2);
+    double sa, ca;
+    pm_sincos(al, &sa, &ca);
     double E22h = (E2 * E2) / 2, E1E2 = E1 * E2, E11 = E1 * E1;
     double a = E22h, b = E22h * ca, c = E1E2 * sa, d = E11 * ca, cp = -c / 2;
     const int Dy = ETL, Dz = 2 * ETL;
@@ -313,11 +332,12 @@ static void epg_vec(int ETL, double alpha_deg, double TE, double T2, double T1, 
     memset(work, 0, sizeof(v3) * 2 * ETL);
     double A = alpha_deg / 180;
     double a1r = (A * 180) * D2R, air = (A * beta) * D2R;
-    double E1 = exp(-(TE / 2) / T1), E2 = exp(-(TE / 2) / T2);
-    double sh = sin(a1r / 2), ch = cos(a1r / 2);
+    double E1 = pm_exp(-(TE / 2) / T1), E2 = pm_exp(-(TE / 2) / T2);
+    double sh, ch, sai, cai;
+    pm_sincos(a1r / 2, &sh, &ch);
+    pm_sincos(air, &sai, &cai);
     double sh2 = sh * sh, ch2 = ch * ch;
     double sa1 = 2 * sh * ch;
-    double sai = sin(air), cai = cos(air);
     double chi2 = (1 + cai) / 2, shi2 = 1 - chi2;
     double a1 = (E2 * E2) * ch2, b1 = (E2 * E2) * sh2, c1 = (E1 * E2) * sa1;
     double ai = (E2 * E2) * chi2, bi = (E2 * E2) * shi2, ci = (E1 * E2) * sai, di = (E1 * E1) * cai;
@@ -397,8 +417,9 @@ static void epg_flat_dual(int ETL, double alpha_deg, double TE, double T2, doubl
     dual *M1 = work, *M2 = work + 3 * ETL, *t;
     for (int i = 0; i < 6 * ETL; ++i) work[i] = dc_(0);
     dual al = {alpha_deg * D2R, D2R};
-    double E1 = exp(-(TE / 2) / T1), E2 = exp(-(TE / 2) / T2);
-    double s = sin(al.v), co = cos(al.v);
+    double E1 = pm_exp(-(TE / 2) / T1), E2 = pm_exp(-(TE / 2) / T2);
+    double s, co;
+    pm_sincos(al.v, &s, &co);
     dual sa = {s, co * al.d}, ca = {co, -s * al.d};
     double E22h = (E2 * E2) / 2, E1E2 = E1 * E2, E11 = E1 * E1;
     dual a = dc_(E22h), b = dmuls(ca, E22h), c = dmuls(sa, E1E2), d = dmuls(ca, E11), cp = ddivs(dneg(c), 2);
@@ -446,7 +467,7 @@ static void epg_flat_dual(int ETL, double alpha_deg, double TE, double T2, doubl
 #undef M1_
 #undef M2_
     /* m0 = sind(alpha/2); d/dalpha = (pi/180) cosd(alpha/2) / 2 */
-    dual m0 = {orc_sind(alpha_deg / 2), D2R * cos((alpha_deg / 2) * D2R) * 0.5};
+    dual m0 = {orc_sind(alpha_deg / 2), D2R * pm_cos((alpha_deg / 2) * D2R) * 0.5};
     for (int i = 0; i < ETL; ++i) {
         dual r = dabs(dmul(m0, dc[i]));
         dcv[i] = r.v;
@@ -463,12 +484,15 @@ static void epg_vec_dual(int ETL, double alpha_deg, double TE, double T2, double
     dual alpha = {alpha_deg, 1.0};
     dual A = ddivs(alpha, 180);
     dual a1r = dmuls(dmuls(A, 180), D2R), air = dmuls(dmuls(A, beta), D2R);
-    double E1 = exp(-(TE / 2) / T1), E2 = exp(-(TE / 2) / T2);
+    double E1 = pm_exp(-(TE / 2) / T1), E2 = pm_exp(-(TE / 2) / T2);
     dual h = ddivs(a1r, 2);
-    dual sh = {sin(h.v), cos(h.v) * h.d}, ch = {cos(h.v), -sin(h.v) * h.d};
+    double shv, chv, saiv, caiv;
+    pm_sincos(h.v, &shv, &chv);
+    pm_sincos(air.v, &saiv, &caiv);
+    dual sh = {shv, chv * h.d}, ch = {chv, -shv * h.d};
     dual sh2 = dmul(sh, sh), ch2 = dmul(ch, ch);
     dual sa1 = dmul(dmuls(sh, 2), ch);
-    dual sai = {sin(air.v), cos(air.v) * air.d}, cai = {cos(air.v), -sin(air.v) * air.d};
+    dual sai = {saiv, caiv * air.d}, cai = {caiv, -saiv * air.d};
     dual chi2 = ddivs(dadd(dc_(1), cai), 2), shi2 = dsub(dc_(1), chi2);
     dual a1 = dmuls(ch2, E2 * E2), b1 = dmuls(sh2, E2 * E2), c1 = dmuls(sa1, E1 * E2);
     dual ai = dmuls(chi2, E2 * E2), bi = dmuls(shi2, E2 * E2), ci = dmuls(sai, E1 * E2), di = dmuls(cai, E1 * E1);
@@ -634,16 +658,17 @@ static void nnls_ws_free(nnls_ws *ws) {
 static double cah(double *A, int lda, double *b, int ip, int jp, int m) {
     if (ip > m) return 0;
     double alpha = Aij(ip, jp);
-    double xnorm = 0;
-    for (int i = ip; i <= m; ++i) xnorm = fma(Aij(i, jp), Aij(i, jp), xnorm);
-    xnorm = sqrt(xnorm);
+    lacc La = {{0}};
+    for (int i = ip; i <= m; ++i) La.p[(i - ip) & 31] = fma(Aij(i, jp), Aij(i, jp), La.p[(i - ip) & 31]);
+    double xnorm = sqrt(lacc_tree(&La));
     FL(2 * (m - ip + 1) + 1);
     if (xnorm == 0) return -1;
     double beta = copysign(xnorm, alpha);
     alpha = alpha + beta;
     double tau = alpha / beta;
-    double sm = V1(b, ip);
-    for (int i = ip + 1; i <= m; ++i) sm = fma(V1(b, i), Aij(i, jp) / alpha, sm);
+    lacc Lb = {{0}};
+    for (int i = ip + 1; i <= m; ++i) Lb.p[(i - ip - 1) & 31] = fma(V1(b, i), Aij(i, jp) / alpha, Lb.p[(i - ip - 1) & 31]);
+    double sm = V1(b, ip) + lacc_tree(&Lb);
     sm *= -tau;
     double A1 = -beta;
     double b1 = V1(b, ip) + sm;
@@ -876,14 +901,18 @@ static void nnls_unsafe(nnls_ws *ws, int init_dual, int max_iter) {
         for (int i = 1; i <= nsetp; ++i) V1(x, V1(idx, i)) = V1(zz, i);
     }
     for (int i = 1; i <= n; ++i) ws->invidx[V1(idx, i) - 1] = i;
-    double sm = 0;
+    lacc Lr = {{0}};
     if (nsetp < m) {
-        for (int i = nsetp + 1; i <= m; ++i) { double bi = V1(b, i); V1(zz, i) = bi; sm = fma(bi, bi, sm); }
+        for (int i = nsetp + 1; i <= m; ++i) {
+            double bi = V1(b, i);
+            V1(zz, i) = bi;
+            Lr.p[(i - nsetp - 1) & 31] = fma(bi, bi, Lr.p[(i - nsetp - 1) & 31]);
+        }
         FL(2 * (m - nsetp));
     } else {
         memset(w, 0, sizeof(double) * n);
     }
-    ws->rnorm = sqrt(sm);
+    ws->rnorm = sqrt(lacc_tree(&Lr));
     ws->nsetp = nsetp;
 }
 
@@ -944,14 +973,18 @@ static void nnls_unsafe_tikh(nnls_ws *ws, double lambda, int init_dual, int max_
         for (int i = 1; i <= nsetp; ++i) V1(x, V1(idx, i)) = V1(zz, i);
     }
     for (int i = 1; i <= n; ++i) ws->invidx[V1(idx, i) - 1] = i;
-    double sm = 0;
+    lacc Lr = {{0}};
     if (nsetp < M) {
-        for (int i = nsetp + 1; i <= M; ++i) { double bi = V1(b, i); V1(zz, i) = bi; sm = fma(bi, bi, sm); }
+        for (int i = nsetp + 1; i <= M; ++i) {
+            double bi = V1(b, i);
+            V1(zz, i) = bi;
+            Lr.p[(i - nsetp - 1) & 31] = fma(bi, bi, Lr.p[(i - nsetp - 1) & 31]);
+        }
         FL(2 * (M - nsetp));
     } else {
         memset(w, 0, sizeof(double) * N);
     }
-    ws->rnorm = sqrt(sm);
+    ws->rnorm = sqrt(lacc_tree(&Lr));
     ws->nsetp = nsetp;
 }
 #undef Aij
@@ -963,10 +996,11 @@ static void nnls_unsafe_tikh(nnls_ws *ws, double lambda, int init_dual, int max_
 static void nnlsprob_solve(nnls_ws *ws, const double *A, int m, int n, const double *b) {
     double *C = ws->A, *f = ws->b, *x = ws->x, *w = ws->w, *z = ws->zz;
     const double *An = A + (size_t)(n - 1) * m;
-    double den = 0;
-    for (int i = 0; i < m; ++i) den += An[i] * An[i];
-    double xj = 0;
-    for (int i = 0; i < m; ++i) xj += (An[i] / den) * b[i];
+    lacc Ld = {{0}}, Lx = {{0}};
+    for (int i = 0; i < m; ++i) Ld.p[i & 31] = Ld.p[i & 31] + An[i] * An[i];
+    double den = lacc_tree(&Ld);
+    for (int i = 0; i < m; ++i) Lx.p[i & 31] = Lx.p[i & 31] + (An[i] / den) * b[i];
+    double xj = lacc_tree(&Lx);
     for (int i = 0; i < m; ++i) z[i] = b[i] - An[i] * xj;
     for (int j = 0; j < n - 1; ++j) {
         double wj = 0;
@@ -989,11 +1023,12 @@ static void nnlsprob_solve_tikh(nnls_ws *ws, const double *A, int m, int n, cons
     const int M = m + n;
     double *C = ws->A, *f = ws->b, *x = ws->x, *w = ws->w, *z = ws->zz;
     const double *An = A + (size_t)(n - 1) * m;
-    double den = 0;
-    for (int i = 0; i < m; ++i) den += An[i] * An[i];
-    den += mu * mu;
-    double xj = 0;
-    for (int i = 0; i < m; ++i) xj += (An[i] / den) * b[i];
+    lacc Ld = {{0}}, Lx = {{0}};
+    for (int i = 0; i < m; ++i) Ld.p[i & 31] = Ld.p[i & 31] + An[i] * An[i];
+    double den = lacc_tree(&Ld);
+    den = den + mu * mu;
+    for (int i = 0; i < m; ++i) Lx.p[i & 31] = Lx.p[i & 31] + (An[i] / den) * b[i];
+    double xj = lacc_tree(&Lx);
     for (int i = 0; i < m; ++i) z[i] = b[i] - An[i] * xj;
     for (int j = 0; j < n - 1; ++j) {
         double wj = 0;
@@ -1017,10 +1052,10 @@ static void nnlsprob_solve_tikh(nnls_ws *ws, const double *A, int m, int n, cons
 /* Tikhonov quantities, src/lsqnonneg.jl:307-318 */
 static inline double tikh_loss(const nnls_ws *ws) { return ws->rnorm * ws->rnorm; }
 static double tikh_seminorm_sq(const nnls_ws *ws) {
-    double s = 0;
-    for (int i = 0; i < ws->nsetp; ++i) { double v = ws->x[ws->idx[i] - 1]; s += v * v; }
+    lacc L = {{0}};
+    for (int i = 0; i < ws->nsetp; ++i) { double v = ws->x[ws->idx[i] - 1]; L.p[i & 31] = L.p[i & 31] + v * v; }
     FL(2 * ws->nsetp);
-    return s;
+    return lacc_tree(&L);
 }
 static double tikh_resnorm_sq(const nnls_ws *ws, double mu) {
     double reg = (mu * mu) * tikh_seminorm_sq(ws);
@@ -1195,8 +1230,13 @@ static void jacobi_svdvals(const double *A, int m, int n, double *s, double *U) 
         for (int p = 0; p < c - 1; ++p) {
             for (int q = p + 1; q < c; ++q) {
                 double *up = U + (size_t)p * r, *uq = U + (size_t)q * r;
-                double al = 0, be = 0, ga = 0;
-                for (int i = 0; i < r; ++i) { al += up[i] * up[i]; be += uq[i] * uq[i]; ga += up[i] * uq[i]; }
+                lacc La = {{0}}, Lb = {{0}}, Lc = {{0}};
+                for (int i = 0; i < r; ++i) {
+                    La.p[i & 31] = fma(up[i], up[i], La.p[i & 31]);
+                    Lb.p[i & 31] = fma(uq[i], uq[i], Lb.p[i & 31]);
+                    Lc.p[i & 31] = fma(up[i], uq[i], Lc.p[i & 31]);
+                }
+                double al = lacc_tree(&La), be = lacc_tree(&Lb), ga = lacc_tree(&Lc);
                 FL(6.0 * r);
                 if (ga == 0 || fabs(ga) <= EPS64 * sqrt(al * be)) continue;
                 double rel = fabs(ga) / sqrt(al * be);
@@ -1215,10 +1255,10 @@ static void jacobi_svdvals(const double *A, int m, int n, double *s, double *U) 
         if (off <= EPS64) break;
     }
     for (int j = 0; j < c; ++j) {
-        double ss = 0;
+        lacc Ls = {{0}};
         const double *u = U + (size_t)j * r;
-        for (int i = 0; i < r; ++i) ss += u[i] * u[i];
-        s[j] = sqrt(ss);
+        for (int i = 0; i < r; ++i) Ls.p[i & 31] = fma(u[i], u[i], Ls.p[i & 31]);
+        s[j] = sqrt(lacc_tree(&Ls));
     }
     qsort(s, c, sizeof(double), cmp_desc);
 }
@@ -1279,7 +1319,7 @@ static inline double tikh_res2(const reg_ws *r) { return tikh_resnorm_sq(&r->tk,
 static double chi2_f(double logmu, void *ctx) {
     reg_ws *r = (reg_ws *)ctx;
     int st = g_st; g_st = ORC_ST_REG_NNLS;
-    reg_solve_tikh(r, exp(logmu));
+    reg_solve_tikh(r, pm_exp(logmu));
     g_st = st;
     double res2 = tikh_res2(r);
     FL(3);
@@ -1307,7 +1347,7 @@ static const double *reg_chi2(reg_ws *r, double chi2_target, double *mu_out, dou
     }
     double mu, res2;
     if (jisfinite(relerr)) {
-        mu = exp(logmu);
+        mu = pm_exp(logmu);
         res2 = r->res2_target * (1 + relerr);
         g_st = ORC_ST_REG_NNLS;
         reg_solve_tikh(r, mu);
@@ -1326,7 +1366,7 @@ static const double *reg_chi2(reg_ws *r, double chi2_target, double *mu_out, dou
 static double mdp_f(double logmu, void *ctx) {
     reg_ws *r = (reg_ws *)ctx;
     int st = g_st; g_st = ORC_ST_REG_NNLS;
-    reg_solve_tikh(r, exp(logmu));
+    reg_solve_tikh(r, pm_exp(logmu));
     g_st = st;
     return tikh_res2(r) - r->delta2;
 }
@@ -1340,8 +1380,9 @@ static const double *reg_mdp(reg_ws *r, double delta, double *mu_out, double *ch
     double res2_min = unreg_res2(r);
     if (delta <= sqrt(res2_min)) { *mu_out = 0; *chi2_out = 1; return r->un.x; }
     /* sum(abs2, work.nnls_prob.b): the problem's (unmodified) data vector */
-    double res2_max = 0;
-    for (int i = 0; i < r->m; ++i) res2_max += r->b[i] * r->b[i];
+    lacc Lm = {{0}};
+    for (int i = 0; i < r->m; ++i) Lm.p[i & 31] = Lm.p[i & 31] + r->b[i] * r->b[i];
+    double res2_max = lacc_tree(&Lm);
     if (delta >= sqrt(res2_max)) {
         memset(zero_n, 0, sizeof(double) * r->n);
         *mu_out = INFINITY; *chi2_out = res2_max / res2_min;
@@ -1360,7 +1401,7 @@ static const double *reg_mdp(reg_ws *r, double delta, double *mu_out, double *ch
     }
     double mu, res2;
     if (jisfinite(err)) {
-        mu = exp(logmu);
+        mu = pm_exp(logmu);
         res2 = delta * delta + err;
         g_st = ORC_ST_REG_NNLS;
         reg_solve_tikh(r, mu);
@@ -1525,16 +1566,16 @@ static double lcurve_corner_impl(lc_ctx *c, double xlow, double xhigh, double xt
 static void lcurve_point(double logmu, double *P, void *ctx) {
     reg_ws *r = (reg_ws *)ctx;
     int st = g_st; g_st = ORC_ST_REG_NNLS;
-    reg_solve_tikh(r, exp(logmu));
+    reg_solve_tikh(r, pm_exp(logmu));
     g_st = st;
-    P[0] = log(tikh_res2(r));
-    P[1] = log(tikh_seminorm_sq(&r->tk));
+    P[0] = pm_log(tikh_res2(r));
+    P[1] = pm_log(tikh_seminorm_sq(&r->tk));
 }
 static const double *reg_lcurve(reg_ws *r, double *mu_out, double *chi2_out, int need_chi2) {
     g_st = ORC_ST_REG_OTHER;
     lc_ctx c = {lcurve_point, r, r};
     double logmu = lcurve_corner_impl(&c, -8.0, 2.0, 1e-4, 1e-4, 1e-4, NULL);
-    double mu = exp(logmu);
+    double mu = pm_exp(logmu);
     g_st = ORC_ST_REG_NNLS;
     reg_solve_tikh(r, mu);
     double chi2 = NAN;
@@ -1559,7 +1600,7 @@ static double gcv_dof(int m, int n, const double *g, double lam) {
 }
 static double gcv_logf(double logmu, void *ctx) {
     reg_ws *r = (reg_ws *)ctx;
-    double mu = exp(logmu);
+    double mu = pm_exp(logmu);
     int st = g_st; g_st = ORC_ST_REG_NNLS;
     reg_solve_tikh(r, mu);
     g_st = st;
@@ -1568,7 +1609,7 @@ static double gcv_logf(double logmu, void *ctx) {
     double G = res2 / (dof * dof);
     double low = (EPS64 * EPS64) / r->m;
     FL(4);
-    return log(jmax(G, low));
+    return pm_log(jmax(G, low));
 }
 static const double *reg_gcv(reg_ws *r, double *mu_out, double *chi2_out, int need_chi2) {
     g_st = ORC_ST_SVD;
@@ -1576,7 +1617,7 @@ static const double *reg_gcv(reg_ws *r, double *mu_out, double *chi2_out, int ne
     g_st = ORC_ST_REG_OTHER;
     double logmu, logG;
     brent_minimize(gcv_logf, r, -8.0, 2.0, 0.0, 1e-4, 20, &logmu, &logG);
-    double mu = exp(logmu);
+    double mu = pm_exp(logmu);
     g_st = ORC_ST_REG_NNLS;
     reg_solve_tikh(r, mu);
     double chi2 = NAN;
@@ -1655,8 +1696,9 @@ static void fa_update(fa_search *s, int I) {
     for (int i = 0; i < m; ++i) s->dAx[i] = 0;
     for (int j = 0; j < n; ++j)
         if (x[j] > 0) { for (int i = 0; i < m; ++i) s->dAx[i] = fma(x[j], dA[i + (size_t)j * m], s->dAx[i]); FL(2 * m); }
-    double dt = 0;
-    for (int i = 0; i < m; ++i) dt = fma(s->dAx[i], s->Axb[i], dt);
+    lacc Lg = {{0}};
+    for (int i = 0; i < m; ++i) Lg.p[i & 31] = fma(s->dAx[i], s->Axb[i], Lg.p[i & 31]);
+    double dt = lacc_tree(&Lg);
     FL(3 * m + 2);
     s->seen[I - 1] = 1;
     s->u[I - 1] = ell;
@@ -1853,23 +1895,23 @@ static void voxel(const t2map_plan *p, vox_ws *w, const double *image, long V, l
     for (int j = 0; j < n; ++j)
         for (int i = 0; i < m; ++i) w->fit[i] = fma(w->A[i + (size_t)j * m], dist[j], w->fit[i]);
     for (int i = 0; i < m; ++i) w->res[i] = w->fit[i] - w->b[i];
-    double sd = 0, sr2 = 0, sr = 0;
-    for (int j = 0; j < n; ++j) sd += dist[j];
-    for (int i = 0; i < m; ++i) sr2 += w->res[i] * w->res[i];
-    for (int i = 0; i < m; ++i) sr += w->res[i];
-    double mean = sr / m, var = 0;
-    for (int i = 0; i < m; ++i) { double d = w->res[i] - mean; var += d * d; }
+    lacc Lsd = {{0}}, Lr2 = {{0}}, Lsr = {{0}}, Ldl = {{0}}, Lv = {{0}}, Lg = {{0}};
+    for (int j = 0; j < n; ++j) Lsd.p[j & 31] = Lsd.p[j & 31] + dist[j];
+    for (int i = 0; i < m; ++i) Lr2.p[i & 31] = Lr2.p[i & 31] + w->res[i] * w->res[i];
+    for (int i = 0; i < m; ++i) Lsr.p[i & 31] = Lsr.p[i & 31] + w->res[i];
+    for (int j = 0; j < n; ++j) Ldl.p[j & 31] = Ldl.p[j & 31] + dist[j] * p->logt2[j];
+    double sd = lacc_tree(&Lsd), sr2 = lacc_tree(&Lr2), sr = lacc_tree(&Lsr), dotl = lacc_tree(&Ldl);
+    double mean = sr / m;
+    for (int i = 0; i < m; ++i) { double d = w->res[i] - mean; Lv.p[i & 31] = Lv.p[i & 31] + d * d; }
+    double var = lacc_tree(&Lv);
     double sigres = sqrt(var / (m - 1));
-    double dotl = 0;
-    for (int j = 0; j < n; ++j) dotl += dist[j] * p->logt2[j];
     double lggm = dotl / sd;
-    double lgva = 0;
-    for (int j = 0; j < n; ++j) { double d = p->logt2[j] - lggm; lgva += (d * d) * dist[j]; }
-    lgva /= sd;
+    for (int j = 0; j < n; ++j) { double d = p->logt2[j] - lggm; Lg.p[j & 31] = Lg.p[j & 31] + (d * d) * dist[j]; }
+    double lgva = lacc_tree(&Lg) / sd;
     FL(4.0 * m * n + 12.0 * m + 8.0 * n + 20);
     if (out->gdn) out->gdn[v] = sd;
-    if (out->ggm) out->ggm[v] = exp(lggm);
-    if (out->gva) out->gva[v] = expm1(lgva);
+    if (out->ggm) out->ggm[v] = pm_exp(lggm);
+    if (out->gva) out->gva[v] = pm_expm1(lgva);
     if (out->fnr) out->fnr[v] = sd / sqrt(sr2 / (m - 1));
     if (out->snr) out->snr[v] = mx / sigres;
     if (out->alpha) out->alpha[v] = alpha;
@@ -2013,8 +2055,8 @@ int orc_t2part(const orc_t2part_opts *o, const double *dist, long V, orc_t2part_
             }
             out->mfr[v] = smp / sd;
         }
-        if (ssp > 0) out->sgm[v] = exp(dsp / ssp);
-        if (smp > 0) out->mgm[v] = exp(dmp / smp);
+        if (ssp > 0) out->sgm[v] = pm_exp(dsp / ssp);
+        if (smp > 0) out->mgm[v] = pm_exp(dmp / smp);
         FL(4.0 * n + 8);
     }
     free(t2); free(lt2); free(wts);
