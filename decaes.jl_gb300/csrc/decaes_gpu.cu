@@ -86,7 +86,7 @@ __global__ void k_compact(const void *image, int f32, long V, double thr, int *v
 }
 
 // Persistent voxel solver: one warp per voxel, voxels pulled from a counter.
-__global__ void __launch_bounds__(32) k_voxels(Params P) {
+__global__ void __launch_bounds__(32) k_voxels(const __grid_constant__ Params P) {
     extern __shared__ double smem[];
     Warp w;
     w.P = &P;
@@ -102,11 +102,20 @@ __global__ void __launch_bounds__(32) k_voxels(Params P) {
     w.s.x = p; p += n;
     w.s.w = p; p += n;
     w.xout = p; p += n;
+    w.s.rdiag = p; p += n;
     p += 8;
     w.s.idx = reinterpret_cast<int *>(p);
-    w.s.diag = reinterpret_cast<unsigned char *>(w.s.idx + 2 * n);
+    w.s.posof = w.s.idx + n;
+    w.s.zl = w.s.posof + n;
+    w.s.diag = reinterpret_cast<unsigned char *>(w.s.zl + 2 * n);
     w.s.lda = lda;
     w.scr = P.scratch + (long)blockIdx.x * P.scr_stride;
+    {
+        const int mn = P.m < P.n ? P.m : P.n;
+        w.sol_key = w.scr + (long)P.m * n + 3L * P.K + (long)kCacheCap * 19 + mn + 16;
+        w.sol_x = w.sol_key + kSolCap;
+        w.nsol = 0;
+    }
     const int nvox = *P.nvox;
     for (;;) {
         int t = 0;

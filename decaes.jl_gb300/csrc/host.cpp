@@ -150,21 +150,37 @@ double erfinv(double x) {
 std::string jlfmt(double v) {
     if (std::isnan(v)) return "NaN";
     if (std::isinf(v)) return v > 0 ? "Inf" : "-Inf";
+    if (v == 0) return std::signbit(v) ? "-0.0" : "0.0";
+    // shortest round-trip digits, then Julia's layout: plain decimal for
+    // 1e-4 <= |v| < 1e6, otherwise d.ddd e<exp> (e.g. 190.0, 0.01, 1.0e-5, 1.0e6)
     char buf[64];
-    for (int p = 1; p <= 17; ++p) {
-        std::snprintf(buf, sizeof buf, "%.*g", p, v);
+    int p = 1;
+    for (; p <= 17; ++p) {
+        std::snprintf(buf, sizeof buf, "%.*e", p - 1, v);
         if (std::strtod(buf, nullptr) == v) break;
     }
     std::string s(buf);
-    size_t e = s.find('e');
-    std::string mant = e == std::string::npos ? s : s.substr(0, e);
-    std::string ex = e == std::string::npos ? "" : s.substr(e + 1);
-    if (mant.find('.') == std::string::npos) mant += ".0";
-    if (!ex.empty()) {
-        int k = std::atoi(ex.c_str());
-        return mant + "e" + std::to_string(k);
+    size_t epos = s.find('e');
+    int E = std::atoi(s.c_str() + epos + 1);
+    std::string mant = s.substr(0, epos);
+    bool neg = mant[0] == '-';
+    if (neg) mant = mant.substr(1);
+    std::string digits;
+    for (char ch : mant) if (ch != '.') digits += ch;
+    std::string out;
+    if (E >= -4 && E < 6) {
+        if (E >= 0) {
+            std::string ip = digits.substr(0, std::min<size_t>(digits.size(), E + 1));
+            while ((int)ip.size() < E + 1) ip += '0';
+            std::string fp = (int)digits.size() > E + 1 ? digits.substr(E + 1) : "0";
+            out = ip + "." + fp;
+        } else {
+            out = "0." + std::string(-E - 1, '0') + digits;
+        }
+    } else {
+        out = digits.substr(0, 1) + "." + (digits.size() > 1 ? digits.substr(1) : "0") + "e" + std::to_string(E);
     }
-    return mant;
+    return neg ? "-" + out : out;
 }
 static std::string nothing_or(double v) { return std::isnan(v) ? "nothing" : jlfmt(v); }
 

@@ -45,6 +45,18 @@ __device__ __forceinline__ double jmin(double x, double y) {
     return signbit(x - y) ? x : y;
 }
 
+// Order-preserving integer image of a double for comparisons on the integer
+// pipes (the FP64 pipe is the kernel's bottleneck): for non-NaN a, b,
+// okey(a) < okey(b) iff a < b, with -0.0 and +0.0 mapped to the same key.
+__device__ __forceinline__ long long okey(double d) {
+    long long b = __double_as_longlong(d);
+    if ((b << 1) == 0) return 0;
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool isnan_bits(double d) {
+    return (__double_as_longlong(d) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+
 // Per-warp views of the NNLS workspace (shared memory).
 struct NnlsWS {
     double *C;    // lda x n, physical columns
@@ -54,8 +66,41 @@ struct NnlsWS {
     double *w;    // n, indexed by logical position (0-based)
     int *idx;     // n, 1-based original column at each logical position
     unsigned char *diag;  // n, indexed by original column
+    double *rdiag;        // n, RN(1/diagonal) of each physical column in set P
+    int *posof;           // n, 1-based logical position of each physical column (inverse of idx)
+    int *zl;              // n, scratch list of physical columns
     int lda;
 };
+
+// Physical columns whose logical position is >= jfirst, in increasing
+// physical order, written to s.zl; returns their count.  Column-parallel
+// loops walk this list so the lanes of a half-warp read distinct bank pairs
+// (odd leading dimension), instead of the random physical columns that the
+// logical order would give.
+__device__ __forceinline__ int warp_active_cols(const NnlsWS &s, int n, int jfirst) {
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    for (int c = 0; c < n; c += 32) {
+        int p = c + lane;
+        bool z = p < n && s.posof[p] >= jfirst;
+        unsigned msk = __ballot_sync(0xffffffffu, z);
+        if (z) s.zl[base + __popc(msk & ((1u << lane) - 1))] = p;
+        base += __popc(msk);
+    }
+    __syncwarp();
+    return base;
+}
+
+// a / b from r = RN(1/b): q = RN(a r), remainder e = a - b q (exact by fma),
+// q' = RN(q + e r).  Markstein's correction (P. Markstein, IBM J. Res. Dev.
+// 34(1), 1990) returns the correctly rounded quotient for normal operands, so
+// results are bitwise those of a / b at three FP64 operations instead of a
+// full division.
+__device__ __forceinline__ double mdiv(double a, double b, double r) {
+    double q = __dmul_rn(a, r);
+    double e = fma(-q, b, a);
+    return fma(e, r, q);
+}
 
 __device__ __forceinline__ double &Aat(const NnlsWS &s, int i1, int j1) {
     // 1-based row i1 of logical column j1
@@ -96,11 +141,13 @@ __device__ double warp_cah(const NnlsWS &s, int ip, int jp, int m) {
     if (xnorm == 0) return -1.0;
     double beta = copysign(xnorm, alpha);
     alpha = alpha + beta;
-    double tau = alpha / beta;
+    const double rbeta = 1.0 / beta;
+    double tau = mdiv(alpha, beta, rbeta);
+    const double ralpha = 1.0 / alpha;
     // quotients A[i,jp]/alpha, staged in zz (free between solves of the main loop)
     part = 0.0;
     for (int i = ip + 1 + lane; i <= m; i += 32) {
-        double qi = col[i - 1] / alpha;
+        double qi = mdiv(col[i - 1], alpha, ralpha);
         s.zz[i - 1] = qi;
         part = fma(s.b[i - 1], qi, part);
     }
@@ -108,7 +155,11 @@ __device__ double warp_cah(const NnlsWS &s, int ip, int jp, int m) {
     sm *= -tau;
     double A1 = -beta;
     double b1 = s.b[ip - 1] + sm;
-    if (b1 / A1 > 0) {
+    // b1 / A1 > 0: same nonzero sign and no underflow of the quotient
+    bool good;
+    if (b1 != 0 && fabs(b1) > 0x1p-900 * fabs(A1)) good = (b1 > 0) == (A1 > 0);
+    else good = b1 / A1 > 0;
+    if (good) {
         if (ip < m) {
             __syncwarp();
             for (int i = ip + 1 + lane; i <= m; i += 32) {
@@ -116,13 +167,18 @@ __device__ double warp_cah(const NnlsWS &s, int ip, int jp, int m) {
                 col[i - 1] = qi;
                 s.b[i - 1] = fma(sm, qi, s.b[i - 1]);
             }
+            const double rA1 = -rbeta;  // 1 / (-beta), exact negation
             if (lane == 0) {
                 s.b[ip - 1] = b1;
                 col[ip - 1] = A1;
+                s.rdiag[s.idx[jp - 1] - 1] = rA1;
             }
             __syncwarp();
         } else {
             tau = 0.0;  // column swap only: done by the caller's idx swap
+            const double rd = 1.0 / col[ip - 1];
+            if (lane == 0) s.rdiag[s.idx[jp - 1] - 1] = rd;
+            __syncwarp();
         }
         return tau;
     }
@@ -135,10 +191,12 @@ __device__ void warp_ahd(const NnlsWS &s, int n, double tau, int j1, int m1) {
     const int lane = threadIdx.x & 31;
     if (j1 >= m1) return;
     const double *u = s.C + (size_t)(s.idx[j1 - 1] - 1) * s.lda;  // u[j1-1] is the diagonal; treated as 1
-    for (int jb = j1 + 1; jb <= n; jb += 32) {
-        int j = jb + lane;
-        if (j <= n) {
-            double *a = s.C + (size_t)(s.idx[j - 1] - 1) * s.lda;
+    const int nz = warp_active_cols(s, n, j1 + 1);
+    for (int r0 = 0; r0 < nz; r0 += 32) {
+        int r = r0 + lane;
+        if (r < nz) {
+            const int p = s.zl[r];
+            double *a = s.C + (size_t)p * s.lda;
             double sm = fma(a[j1 - 1], 1.0, 0.0);
             for (int i = j1 + 1; i <= m1; ++i) sm = fma(a[i - 1], u[i - 1], sm);
             sm *= -tau;
@@ -149,7 +207,7 @@ __device__ void warp_ahd(const NnlsWS &s, int n, double tau, int j1, int m1) {
                 wj = fma(v, s.b[i - 1], wj);
                 a[i - 1] = v;
             }
-            s.w[j - 1] = wj;
+            s.w[s.posof[p] - 1] = wj;
         }
     }
     __syncwarp();
@@ -158,13 +216,15 @@ __device__ void warp_ahd(const NnlsWS &s, int n, double tau, int j1, int m1) {
 // compute_dual!(w, A, b, j1, m1), src/NNLS.jl:441-470.  Lanes over columns.
 __device__ void warp_compute_dual(const NnlsWS &s, int n, int j1, int m1) {
     const int lane = threadIdx.x & 31;
-    for (int jb = j1; jb <= n; jb += 32) {
-        int j = jb + lane;
-        if (j <= n) {
-            const double *a = s.C + (size_t)(s.idx[j - 1] - 1) * s.lda;
+    const int nz = warp_active_cols(s, n, j1);
+    for (int r0 = 0; r0 < nz; r0 += 32) {
+        int r = r0 + lane;
+        if (r < nz) {
+            const int p = s.zl[r];
+            const double *a = s.C + (size_t)p * s.lda;
             double sm = 0.0;
             for (int i = j1; i <= m1; ++i) sm = fma(a[i - 1], s.b[i - 1], sm);
-            s.w[j - 1] = sm;
+            s.w[s.posof[p] - 1] = sm;
         }
     }
     __syncwarp();
@@ -177,8 +237,9 @@ __device__ void warp_solve_tri(const NnlsWS &s, int n) {
     for (int i = lane; i < n; i += 32) s.zz[i] = s.b[i];
     __syncwarp();
     for (int j = n; j >= 1; --j) {
-        const double *a = s.C + (size_t)(s.idx[j - 1] - 1) * s.lda;
-        double zi = -s.zz[j - 1] / a[j - 1];
+        const int pj = s.idx[j - 1] - 1;
+        const double *a = s.C + (size_t)pj * s.lda;
+        double zi = -mdiv(s.zz[j - 1], a[j - 1], s.rdiag[pj]);
         for (int i = 1 + lane; i <= j - 1; i += 32) s.zz[i - 1] = fma(a[i - 1], zi, s.zz[i - 1]);
         __syncwarp();
         if (lane == 0) s.zz[j - 1] = -zi;
@@ -201,22 +262,24 @@ __device__ void warp_solve_tri_t(const NnlsWS &s, double *z, int n) {
     }
 }
 
-// Largest positive dual over logical positions j1..n (first maximum wins).
+// Largest positive dual over logical positions j1..n (first maximum wins,
+// as the reference's `w[j] > wmax` scan from wmax = 0).  Positive doubles
+// order like their bit patterns, so the search runs on the integer pipes.
 __device__ __forceinline__ void warp_largest_dual(const NnlsWS &s, int n, int j1, double &wmax, int &jmax) {
     const int lane = threadIdx.x & 31;
-    double wm = 0.0;
+    long long km = 0;
     int jm = 0;
     for (int j = j1 + lane; j <= n; j += 32) {
-        double v = s.w[j - 1];
-        if (v > wm) { wm = v; jm = j; }
+        long long k = __double_as_longlong(s.w[j - 1]);
+        if (k > 0 && k <= 0x7ff0000000000000LL && k > km) { km = k; jm = j; }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        double ow = __shfl_xor_sync(FULL, wm, o);
+        long long ok = __shfl_xor_sync(FULL, km, o);
         int oj = __shfl_xor_sync(FULL, jm, o);
-        if (ow > wm || (ow == wm && oj != 0 && (jm == 0 || oj < jm))) { wm = ow; jm = oj; }
+        if (ok > km || (ok == km && oj != 0 && (jm == 0 || oj < jm))) { km = ok; jm = oj; }
     }
-    wmax = wm;
+    wmax = __longlong_as_double(km);
     jmax = jm;
 }
 
@@ -266,6 +329,8 @@ __device__ NnlsResult warp_nnls(const NnlsWS &s, int M, int n, int m0, bool tikh
             int t = s.idx[nsetp - 1];
             s.idx[nsetp - 1] = s.idx[jmax - 1];
             s.idx[jmax - 1] = t;
+            s.posof[s.idx[nsetp - 1] - 1] = nsetp;
+            s.posof[t - 1] = jmax;
         }
         __syncwarp();
         if (nsetp < n) warp_ahd(s, n, tau, nsetp, m);
@@ -285,21 +350,24 @@ __device__ NnlsResult warp_nnls(const NnlsWS &s, int M, int n, int m0, bool tikh
             int imv = nsetp;
             double alpha = 2.0;
             {
+                long long a_key = okey(2.0);
                 double a_loc = 2.0;
                 int i_loc = 0;
                 for (int i = 1 + lane; i <= nsetp; i += 32) {
                     double zi = s.zz[i - 1];
-                    if (zi <= 0) {
+                    if (!isnan_bits(zi) && okey(zi) <= 0) {
                         double xi = s.x[s.idx[i - 1] - 1];
                         double t = -xi / (zi - xi);
-                        if (a_loc > t) { a_loc = t; i_loc = i; }
+                        long long tk = okey(t);
+                        if (!isnan_bits(t) && a_key > tk) { a_key = tk; a_loc = t; i_loc = i; }
                     }
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
+                    long long ok = __shfl_xor_sync(FULL, a_key, o);
                     double oa = __shfl_xor_sync(FULL, a_loc, o);
                     int oi = __shfl_xor_sync(FULL, i_loc, o);
-                    if (oi != 0 && (i_loc == 0 || oa < a_loc || (oa == a_loc && oi < i_loc))) { a_loc = oa; i_loc = oi; }
+                    if (oi != 0 && (i_loc == 0 || ok < a_key || (ok == a_key && oi < i_loc))) { a_key = ok; a_loc = oa; i_loc = oi; }
                 }
                 if (i_loc != 0) { imv = i_loc; alpha = a_loc; }
             }
@@ -321,16 +389,19 @@ __device__ NnlsResult warp_nnls(const NnlsWS &s, int M, int n, int m0, bool tikh
                         double sg = jl_hypot(a, bb);
                         double cc = a / sg, ss = bb / sg;
                         __syncwarp();
-                        for (int j = 1 + lane; j <= n; j += 32) {
-                            if (j == i) continue;
-                            double *cj = s.C + (size_t)(s.idx[j - 1] - 1) * s.lda;
+                        const int pi = s.idx[i - 1] - 1;
+                        for (int pj = lane; pj < n; pj += 32) {
+                            if (pj == pi) continue;
+                            double *cj = s.C + (size_t)pj * s.lda;
                             double p = cj[i - 2], r = cj[i - 1];
                             cj[i - 2] = fma(cc, p, __dmul_rn(ss, r));
                             cj[i - 1] = fma(-ss, p, __dmul_rn(cc, r));
                         }
+                        const double rsg = 1.0 / sg;
                         if (lane == 0) {
                             ci[i - 2] = sg;
                             ci[i - 1] = 0.0;
+                            s.rdiag[s.idx[i - 1] - 1] = rsg;
                             double p = s.b[i - 2], r = s.b[i - 1];
                             s.b[i - 2] = fma(cc, p, __dmul_rn(ss, r));
                             s.b[i - 1] = fma(-ss, p, __dmul_rn(cc, r));
@@ -340,8 +411,12 @@ __device__ NnlsResult warp_nnls(const NnlsWS &s, int M, int n, int m0, bool tikh
                     // move logical column imv to position nsetp (idx rotation; no data moves)
                     if (lane == 0) {
                         int t = s.idx[imv - 1];
-                        for (int j = imv; j <= nsetp - 1; ++j) s.idx[j - 1] = s.idx[j];
+                        for (int j = imv; j <= nsetp - 1; ++j) {
+                            s.idx[j - 1] = s.idx[j];
+                            s.posof[s.idx[j - 1] - 1] = j;
+                        }
                         s.idx[nsetp - 1] = t;
+                        s.posof[t - 1] = nsetp;
                     }
                     __syncwarp();
                 }
@@ -384,20 +459,23 @@ __device__ NnlsResult warp_nnls(const NnlsWS &s, int M, int n, int m0, bool tikh
 // its Tikhonov form (src/lsqnonneg.jl:86-164): copy A (global, m x n) into
 // the workspace, seed the dual with column n, then run the NNLS loops.
 // `data` is the (shared-memory) right-hand side; it is not modified.
-__device__ NnlsResult warp_lsq(const NnlsWS &s, const double *__restrict__ A, int m, int n, const double *data,
-                               bool tikh, double mu) {
+// Not inlined: every caller shares one copy of the NNLS code (instruction
+// cache), and the workspace views travel in registers.
+__device__ __noinline__ NnlsResult warp_lsq(const NnlsWS s, const double *A, int m, int n, const double *data,
+                                            bool tikh, double mu) {
     const int lane = threadIdx.x & 31;
     const int M = tikh ? m + n : m;
     // C[:, j] = A[:, j] (coalesced), padded rows zeroed
     for (int j = 0; j < n; ++j) {
         const double *aj = A + (size_t)j * m;
         double *cj = s.C + (size_t)j * s.lda;
-        for (int i = lane; i < M; i += 32) cj[i] = (i < m) ? __ldg(aj + i) : 0.0;
+        for (int i = lane; i < M; i += 32) cj[i] = (i < m) ? aj[i] : 0.0;
     }
     for (int i = lane; i < M; i += 32) s.b[i] = (i < m) ? data[i] : 0.0;
     for (int j = lane; j < n; j += 32) {
         s.x[j] = 0.0;
         s.idx[j] = j + 1;
+        s.posof[j] = j + 1;
         s.diag[j] = 0;
     }
     __syncwarp();
@@ -406,8 +484,9 @@ __device__ NnlsResult warp_lsq(const NnlsWS &s, const double *__restrict__ A, in
     for (int i = lane; i < m; i += 32) part = __dadd_rn(part, __dmul_rn(an[i], an[i]));
     double den = wsum(part);
     if (tikh) den = __dadd_rn(den, __dmul_rn(mu, mu));
+    const double rden = 1.0 / den;
     part = 0.0;
-    for (int i = lane; i < m; i += 32) part = __dadd_rn(part, __dmul_rn(an[i] / den, data[i]));
+    for (int i = lane; i < m; i += 32) part = __dadd_rn(part, __dmul_rn(mdiv(an[i], den, rden), data[i]));
     double xj = wsum(part);
     for (int i = lane; i < m; i += 32) s.zz[i] = __dsub_rn(data[i], __dmul_rn(an[i], xj));
     __syncwarp();

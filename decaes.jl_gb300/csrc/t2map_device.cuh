@@ -10,6 +10,7 @@ namespace dk {
 
 constexpr int kCacheCap = 128;   // L-curve cache entries per voxel (the loop needs ~30)
 constexpr int kLoopCap = 512;    // hard cap of every data-dependent outer loop
+constexpr int kSolCap = 64;      // stored Tikhonov solutions per voxel (keyed by log mu)
 
 struct Params {
     int m, n, K, M, lda;
@@ -41,15 +42,15 @@ struct Params {
 
 // Shared-memory footprint of one warp worker (doubles), mirrored on the host.
 __host__ __device__ inline long warp_smem_doubles(int m, int n, int lda) {
-    long d = (long)lda * n + 3L * lda + 3L * n + 8;
-    long ints = 2L * n;            // idx
+    long d = (long)lda * n + 3L * lda + 4L * n + 8;
+    long ints = 4L * n;            // idx, posof, zl
     long bytes = (long)n;          // diag
     return d + (ints * 4 + bytes + 7) / 8;
 }
 // Global scratch of one warp worker (doubles).
 __host__ __device__ inline long warp_scratch_doubles(int m, int n, int K) {
     int mn = m < n ? m : n;
-    return (long)m * n + 3L * K + (long)kCacheCap * (3 + 4 + 12) + mn + 16;
+    return (long)m * n + 3L * K + (long)kCacheCap * (3 + 4 + 12) + mn + 16 + (long)kSolCap * (n + 1);
 }
 
 struct Warp {
@@ -59,11 +60,61 @@ struct Warp {
     double *xout;  // saved solution (shared), n
     double *A;     // per-voxel basis (global scratch), m x n
     double *scr;   // per-warp global scratch base
+    double *sol_key, *sol_x;  // stored Tikhonov solutions: log mu keys, kSolCap x n
+    int nsol;
     int lane;
     unsigned nnls_caps, loop_caps;
 };
 
 __device__ __forceinline__ void note(Warp &w, const NnlsResult &r) { w.nnls_caps += (r.mode != 0); }
+
+// Keys with Julia's isless order (NaN above everything, -0.0 < +0.0), for
+// findmax-style searches on the integer pipes.
+__device__ __forceinline__ long long ilkey(double d) {
+    long long b = __double_as_longlong(d);
+    if ((b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) return 0x7fffffffffffffffLL;
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool isapprox(double x, double y) {
+    if (x == y) return true;
+    if (!(isfinite(x) && isfinite(y))) return false;
+    return fabs(x - y) <= jmax(0.0, 1.4901161193847656e-08 * jmax(fabs(x), fabs(y)));
+}
+// First i in [0, len) with isapprox(x, keys[i]), or -1; lanes over entries.
+__device__ int warp_find_approx(const double *keys, int len, double x) {
+    const int lane = threadIdx.x & 31;
+    for (int c = 0; c < len; c += 32) {
+        int i = c + lane;
+        bool hit = i < len && isapprox(x, keys[i]);
+        unsigned msk = __ballot_sync(FULL, hit);
+        if (msk) return c + __ffs(msk) - 1;
+    }
+    return -1;
+}
+// First i with keys[i] == x exactly (as doubles), or -1.
+__device__ int warp_find_exact(const double *keys, int len, double x) {
+    const int lane = threadIdx.x & 31;
+    for (int c = 0; c < len; c += 32) {
+        int i = c + lane;
+        bool hit = i < len && keys[i] == x;
+        unsigned msk = __ballot_sync(FULL, hit);
+        if (msk) return c + __ffs(msk) - 1;
+    }
+    return -1;
+}
+// Store the current Tikhonov solution s.x under key log mu.
+__device__ void sol_store(Warp &w, double logmu) {
+    if (w.nsol >= kSolCap) return;
+    const int n = w.P->n;
+    double *dst = w.sol_x + (long)w.nsol * n;
+    for (int j = w.lane; j < n; j += 32) dst[j] = w.s.x[j];
+    if (w.lane == 0) w.sol_key[w.nsol] = logmu;
+    __syncwarp();
+    w.nsol++;
+}
+// The solution at mu = exp(logmu): from the store when this exact key was
+// solved before (the solve is deterministic), else solved now.  Result in xout.
+__device__ void final_solution(Warp &w, double logmu);
 
 // ----------------------------------------------------------------------------
 // Tikhonov helpers (src/lsqnonneg.jl:297-318)
@@ -86,6 +137,18 @@ __device__ double tikh_res2(Warp &w, const TikhState &t) {
 __device__ void save_x(Warp &w) {
     for (int j = w.lane; j < w.P->n; j += 32) w.xout[j] = w.s.x[j];
     __syncwarp();
+}
+
+__device__ void final_solution(Warp &w, double logmu) {
+    int i = warp_find_exact(w.sol_key, w.nsol, logmu);
+    if (i >= 0) {
+        const double *src = w.sol_x + (long)i * w.P->n;
+        for (int j = w.lane; j < w.P->n; j += 32) w.xout[j] = src[j];
+        __syncwarp();
+        return;
+    }
+    tikh_solve(w, pm_exp(logmu));
+    save_x(w);
 }
 
 // ----------------------------------------------------------------------------
@@ -219,6 +282,7 @@ struct Chi2F {  // f(logμ) of lsqnonneg_chi2!, src/lsqnonneg.jl:566-569
     double target;
     __device__ double operator()(double logmu) {
         TikhState t = tikh_solve(*w, pm_exp(logmu));
+        sol_store(*w, logmu);
         return (tikh_res2(*w, t) - target) / target;
     }
 };
@@ -227,6 +291,7 @@ struct MdpF {  // f(logμ) of lsqnonneg_mdp!, src/lsqnonneg.jl:723-726
     double delta2;
     __device__ double operator()(double logmu) {
         TikhState t = tikh_solve(*w, pm_exp(logmu));
+        sol_store(*w, logmu);
         return tikh_res2(*w, t) - delta2;
     }
 };
@@ -259,11 +324,11 @@ __device__ void reg_chi2(Warp &w, double chi2_target, double &mu_out, double &ch
     if (isfinite(relerr)) {
         mu = pm_exp(logmu);
         res2 = f.target * (1 + relerr);
-        tikh_solve(w, mu);
+        final_solution(w, logmu);
     } else {
         mu = 0; res2 = 1;  // saved solution: the last Tikhonov solve
+        save_x(w);
     }
-    save_x(w);
     mu_out = mu;
     chi2_out = res2 / res2_min;
 }
@@ -300,11 +365,11 @@ __device__ void reg_mdp(Warp &w, double delta, double &mu_out, double &chi2_out)
     if (isfinite(err)) {
         mu = pm_exp(logmu);
         res2 = delta * delta + err;
-        tikh_solve(w, mu);
+        final_solution(w, logmu);
     } else {
         mu = 0; res2 = 1;
+        save_x(w);
     }
-    save_x(w);
     mu_out = mu;
     chi2_out = res2 / res2_min;
 }
@@ -318,23 +383,13 @@ struct LCurve {
     int flen, plen, slen;
     bool overflow;
 };
-__device__ __forceinline__ bool isapprox(double x, double y) {
-    if (x == y) return true;
-    if (!(isfinite(x) && isfinite(y))) return false;
-    return fabs(x - y) <= jmax(0.0, 1.4901161193847656e-08 * jmax(fabs(x), fabs(y)));
-}
-__device__ __forceinline__ bool jisless(double a, double b) {
-    if (isnan(a)) return false;
-    if (isnan(b)) return true;
-    if (a == b) return signbit(a) && !signbit(b);
-    return a < b;
-}
 // f_lcurve(logμ) = (log ||Ax-b||^2, log ||x||^2) through the isapprox-keyed cache
 __device__ void lc_eval(LCurve &L, double x, double &P0, double &P1) {
-    for (int i = 0; i < L.flen; ++i)
-        if (isapprox(x, L.fx[i])) { P0 = L.fP[2 * i]; P1 = L.fP[2 * i + 1]; return; }
+    int hit = warp_find_approx(L.fx, L.flen, x);
+    if (hit >= 0) { P0 = L.fP[2 * hit]; P1 = L.fP[2 * hit + 1]; return; }
     Warp &w = *L.w;
     TikhState t = tikh_solve(w, pm_exp(x));
+    sol_store(w, x);
     double res2 = tikh_res2(w, t);
     double ssq = warp_seminorm_sq(w.s, t.r.nsetp);
     P0 = pm_log(res2);
@@ -347,10 +402,7 @@ __device__ void lc_eval(LCurve &L, double x, double &P0, double &P1) {
         L.overflow = true;
     }
 }
-__device__ int pc_find(const LCurve &L, double x) {
-    for (int i = 0; i < L.plen; ++i) if (isapprox(x, L.px[i])) return i;
-    return -1;
-}
+__device__ int pc_find(const LCurve &L, double x) { return warp_find_approx(L.px, L.plen, x); }
 __device__ void pc_set(LCurve &L, double x, double P0, double P1, double C, bool push_only) {
     int i = push_only ? -1 : pc_find(L, x);
     if (i < 0) {
@@ -361,12 +413,28 @@ __device__ void pc_set(LCurve &L, double x, double P0, double P1, double C, bool
     if (L.w->lane == 0) { L.pP[2 * i] = P0; L.pP[2 * i + 1] = P1; L.pC[i] = C; }
     __syncwarp();
 }
+// mapfindmax over the point cache's curvatures (first maximum under isless)
 __device__ int pc_argmax(const LCurve &L) {
-    int im = 0;
-    for (int i = 1; i < L.plen; ++i) if (jisless(L.pC[im], L.pC[i])) im = i;
-    return im;
+    const int lane = threadIdx.x & 31;
+    long long bk = 0;
+    int bi = -1;
+    for (int c = 0; c < L.plen; c += 32) {
+        int i = c + lane;
+        if (i < L.plen) {
+            long long k = ilkey(L.pC[i]);
+            if (bi < 0 || k > bk) { bk = k; bi = i; }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        long long ok = __shfl_xor_sync(FULL, bk, o);
+        int oi = __shfl_xor_sync(FULL, bi, o);
+        if (oi >= 0 && (bi < 0 || ok > bk || (ok == bk && oi < bi))) { bk = ok; bi = oi; }
+    }
+    return bi;
 }
 __device__ __forceinline__ double nrm2(double a, double b) { return sqrt(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b))); }
+// menger(Pj, Pk, Pl), src/lsqnonneg.jl:967-972
 __device__ double menger(double j0, double j1, double k0, double k1, double l0, double l1) {
     double djk0 = j0 - k0, djk1 = j1 - k1, dkl0 = k0 - l0, dkl1 = k1 - l1, dlj0 = l0 - j0, dlj1 = l1 - j1;
     double a = __dadd_rn(__dmul_rn(djk0, djk0), __dmul_rn(djk1, djk1));
@@ -378,22 +446,75 @@ __device__ double menger(double j0, double j1, double k0, double k1, double l0, 
 struct LcState {
     double x[4], P[8];
 };
-// update_curvature!, src/lsqnonneg.jl:948-965
+// update_curvature!, src/lsqnonneg.jl:948-965.  The nearest cached
+// neighbours (largest key below x, smallest above; first index on ties) are
+// found lanes-over-entries with integer keys.
 __device__ void lc_update_curvature(LCurve &L, const LcState &s, const double *Ptl, const double *Pbr, double Ctol) {
-    for (int i = 0; i < 4; ++i) {
-        double x = s.x[i], P0 = s.P[2 * i], P1 = s.P[2 * i + 1];
+    const int lane = threadIdx.x & 31;
+    for (int q = 0; q < 4; ++q) {
+        double x = s.x[q], P0 = s.P[2 * q], P1 = s.P[2 * q + 1];
         double C = -CUDART_INF;
         if (jmin(nrm2(P0 - Ptl[0], P1 - Ptl[1]), nrm2(P0 - Pbr[0], P1 - Pbr[1])) > Ctol) {
-            double xm = -CUDART_INF, xp = CUDART_INF, m0 = P0, m1 = P1, p0 = P0, p1 = P1;
-            for (int k = 0; k < L.plen; ++k) {
-                double xk = L.px[k];
-                if (xm < xk && xk < x) { xm = xk; m0 = L.pP[2 * k]; m1 = L.pP[2 * k + 1]; }
-                if (x < xk && xk < xp) { xp = xk; p0 = L.pP[2 * k]; p1 = L.pP[2 * k + 1]; }
+            const long long kx = okey(x);
+            long long km = 0, kp = 0;
+            int im = -1, ip = -1;
+            for (int c = 0; c < L.plen; c += 32) {
+                int i = c + lane;
+                if (i < L.plen) {
+                    long long k = okey(L.px[i]);
+                    if (k < kx && (im < 0 || k > km)) { km = k; im = i; }
+                    if (k > kx && (ip < 0 || k < kp)) { kp = k; ip = i; }
+                }
             }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                long long okm = __shfl_xor_sync(FULL, km, o), okp = __shfl_xor_sync(FULL, kp, o);
+                int oim = __shfl_xor_sync(FULL, im, o), oip = __shfl_xor_sync(FULL, ip, o);
+                if (oim >= 0 && (im < 0 || okm > km || (okm == km && oim < im))) { km = okm; im = oim; }
+                if (oip >= 0 && (ip < 0 || okp < kp || (okp == kp && oip < ip))) { kp = okp; ip = oip; }
+            }
+            double m0 = P0, m1 = P1, p0 = P0, p1 = P1;
+            if (im >= 0) { m0 = L.pP[2 * im]; m1 = L.pP[2 * im + 1]; }
+            if (ip >= 0) { p0 = L.pP[2 * ip]; p1 = L.pP[2 * ip + 1]; }
             C = menger(m0, m1, P0, P1, p0, p1);
         }
         pc_set(L, x, P0, P1, C, false);
     }
+}
+// Backtracking scan of the state cache (src/lsqnonneg.jl:895-899): the
+// sequential loop adopts state k when it contains the best point and its
+// width is <= the width of the state held so far; equivalently, k is adopted
+// iff it matches and its width is <= the running minimum over earlier matches
+// (and the current width).  Returns the last adopted index, or -1.
+__device__ int lc_backtrack(const LCurve &L, double xb, double w0) {
+    const int lane = threadIdx.x & 31;
+    long long carry = __double_as_longlong(w0);  // widths are >= +0: bit order == value order
+    int last = -1;
+    for (int c = 0; c < L.slen; c += 32) {
+        int k = c + lane;
+        bool match = false;
+        long long wk = 0x7fffffffffffffffLL;
+        if (k < L.slen) {
+            const double *sx = L.sx + 4 * k;
+            match = (sx[1] == xb || sx[2] == xb);
+            if (match) wk = __double_as_longlong(fabs(sx[3] - sx[0]));
+        }
+        long long incl = wk;  // inclusive prefix minimum of matched widths
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            long long t = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o && t < incl) incl = t;
+        }
+        long long excl = __shfl_up_sync(FULL, incl, 1);
+        if (lane == 0) excl = 0x7fffffffffffffffLL;
+        long long bound = excl < carry ? excl : carry;
+        bool adopted = match && wk <= bound;
+        unsigned msk = __ballot_sync(FULL, adopted);
+        if (msk) last = c + 31 - __clz(msk);
+        long long tot = __shfl_sync(FULL, incl, 31);
+        if (tot < carry) carry = tot;
+    }
+    return last;
 }
 // lcurve_corner with backtracking, src/lsqnonneg.jl:872-919
 __device__ double lcurve_corner(LCurve &L, double xlow, double xhigh, double xtol, double Ptol, double Ctol) {
@@ -414,12 +535,10 @@ __device__ double lcurve_corner(LCurve &L, double xlow, double xhigh, double xto
         iter += 1;
         if (iter > kLoopCap || L.overflow) { L.w->loop_caps++; break; }
         double xb = L.px[pc_argmax(L)];
-        for (int k = 0; k < L.slen; ++k) {
-            const double *sx = L.sx + 4 * k;
-            if ((sx[1] == xb || sx[2] == xb) && fabs(sx[3] - sx[0]) <= fabs(st.x[3] - st.x[0])) {
-                for (int q = 0; q < 4; ++q) st.x[q] = sx[q];
-                for (int q = 0; q < 8; ++q) st.P[q] = L.sP[8 * k + q];
-            }
+        int kb = lc_backtrack(L, xb, fabs(st.x[3] - st.x[0]));
+        if (kb >= 0) {
+            for (int q = 0; q < 4; ++q) st.x[q] = L.sx[4 * kb + q];
+            for (int q = 0; q < 8; ++q) st.P[q] = L.sP[8 * kb + q];
         }
         int i2 = pc_find(L, st.x[1]), i3 = pc_find(L, st.x[2]);
         if (i2 < 0 || i3 < 0) { L.w->loop_caps++; break; }
@@ -463,14 +582,16 @@ __device__ void reg_lcurve(Warp &w, double &mu_out, double &chi2_out) {
     L.sx = L.pC + kCacheCap; L.sP = L.sx + 4 * kCacheCap;
     double logmu = lcurve_corner(L, -8.0, 2.0, 1e-4, 1e-4, 1e-4);
     double mu = pm_exp(logmu);
-    TikhState t = tikh_solve(w, mu);
-    double res2 = tikh_res2(w, t);
-    save_x(w);
     double chi2 = CUDART_NAN;
     if (w.P->need_chi2) {
+        TikhState t = tikh_solve(w, mu);
+        double res2 = tikh_res2(w, t);
+        save_x(w);
         NnlsResult r0 = warp_lsq(w.s, w.A, w.P->m, w.P->n, w.data, false, 0.0);
         note(w, r0);
         chi2 = res2 / __dmul_rn(r0.rnorm, r0.rnorm);
+    } else {
+        final_solution(w, logmu);
     }
     mu_out = mu;
     chi2_out = chi2;
@@ -542,6 +663,7 @@ struct GcvF {  // log𝒢(logμ), src/lsqnonneg.jl:1150-1154 and gcv!, 1213-1229
         const Params &P = *w->P;
         double mu = pm_exp(logmu);
         TikhState t = tikh_solve(*w, mu);
+        sol_store(*w, logmu);
         double res2 = tikh_res2(*w, t);
         int k = P.m < P.n ? P.m : P.n;
         double dof = (double)(P.m - P.n > 0 ? P.m - P.n : 0), l2 = mu * mu;
@@ -558,14 +680,16 @@ __device__ void reg_gcv(Warp &w, double &mu_out, double &chi2_out) {
     double logmu, logG;
     brent_minimize(f, -8.0, 2.0, 0.0, 1e-4, 20, logmu, logG);
     double mu = pm_exp(logmu);
-    TikhState t = tikh_solve(w, mu);
-    double res2 = tikh_res2(w, t);
-    save_x(w);
     double chi2 = CUDART_NAN;
     if (P.need_chi2) {
+        TikhState t = tikh_solve(w, mu);
+        double res2 = tikh_res2(w, t);
+        save_x(w);
         NnlsResult r0 = warp_lsq(w.s, w.A, P.m, P.n, w.data, false, 0.0);
         note(w, r0);
         chi2 = res2 / __dmul_rn(r0.rnorm, r0.rnorm);
+    } else {
+        final_solution(w, logmu);
     }
     mu_out = mu;
     chi2_out = chi2;
@@ -651,20 +775,21 @@ __device__ void fa_evaluate_box(Search &S, int lo, int hi, bool have_x, double x
 __device__ void fa_initialize(Search &S) {
     const int K = S.w->P->K;
     for (int depth = 1; depth <= S.mineval; ++depth) {
-        int st_lo[64], st_hi[64], st_d[64];
+        // stack of boxes, packed (lo | hi << 9 | depth << 18); 1 <= lo, hi <= 256
+        unsigned st[48];
         int sp = 0;
-        st_lo[0] = 1; st_hi[0] = K; st_d[0] = depth; sp = 1;
+        st[sp++] = 1u | ((unsigned)K << 9) | ((unsigned)depth << 18);
         int guard = 0;
         while (sp > 0 && guard++ < 4096) {
-            --sp;
-            int lo = st_lo[sp], hi = st_hi[sp], d = st_d[sp];
+            unsigned e = st[--sp];
+            int lo = e & 511, hi = (e >> 9) & 511, d = (int)(e >> 18);
             if (d <= 0) continue;
             fa_evaluate_box(S, lo, hi, false, 0.0);
             if (S.numeval >= S.mineval) continue;
             int mid = (lo + hi) / 2;
-            if (sp + 2 > 64) { S.w->loop_caps++; break; }
-            st_lo[sp] = mid; st_hi[sp] = hi; st_d[sp] = d - 1; ++sp;  // right, processed after left
-            st_lo[sp] = lo; st_hi[sp] = mid; st_d[sp] = d - 1; ++sp;
+            if (sp + 2 > 48) { S.w->loop_caps++; break; }
+            st[sp++] = (unsigned)mid | ((unsigned)hi << 9) | ((unsigned)(d - 1) << 18);  // right, after left
+            st[sp++] = (unsigned)lo | ((unsigned)mid << 9) | ((unsigned)(d - 1) << 18);
         }
         if (S.numeval >= S.mineval) break;
     }
@@ -783,6 +908,7 @@ __device__ void warp_basis(Warp &w, double alpha, double *out /* m x n, global *
 __device__ void process_voxel(Warp &w, long v) {
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lane = w.lane;
+    w.nsol = 0;
     // copy + normalize by the maximum echo
     double mx = 0;
     for (int i = lane; i < m; i += 32) {
