@@ -5,53 +5,9 @@
 #pragma once
 #include "epg.cuh"
 #include "nnls_warp.cuh"
+#include "t2map_params.cuh"
 
 namespace dk {
-
-constexpr int kCacheCap = 128;   // L-curve cache entries per voxel (the loop needs ~30)
-constexpr int kLoopCap = 512;    // hard cap of every data-dependent outer loop
-constexpr int kSolCap = 64;      // stored Tikhonov solutions per voxel (keyed by log mu)
-
-struct Params {
-    int m, n, K, M, lda;
-    int reg;
-    double chi2factor, noiselevel;
-    int mineval, maxeval;
-    int angle_mode;  // 0 search, 1 fixed SetFlipAngle, 2 B1 map
-    double fixed_angle;
-    int beta180;
-    double beta, TE, T1;
-    long V;
-    const int *nvox;
-    const int *vidx;
-    const void *image;
-    int image_f32;
-    const void *b1map;
-    const double *t2, *logt2, *angles, *As, *dAs, *basis_fixed;
-    double *scratch;
-    long scr_stride;  // doubles per warp
-    int *counter;
-    unsigned long long *stats;  // [0] NNLS cap hits, [1] loop cap hits
-    double *dist, *gdn, *ggm, *gva, *fnr, *snr, *alpha, *resnorm, *decaycurve, *mu, *chi2f, *basis_out;
-    int fuse_t2part, sp0, sp1, mp0, mp1;
-    const double *weights;
-    double *sfr, *sgm, *mfr, *mgm;
-    int need_chi2;
-    int epg_lanes;
-};
-
-// Shared-memory footprint of one warp worker (doubles), mirrored on the host.
-__host__ __device__ inline long warp_smem_doubles(int m, int n, int lda) {
-    long d = (long)lda * n + 3L * lda + 4L * n + 8;
-    long ints = 4L * n;            // idx, posof, zl
-    long bytes = (long)n;          // diag
-    return d + (ints * 4 + bytes + 7) / 8;
-}
-// Global scratch of one warp worker (doubles).
-__host__ __device__ inline long warp_scratch_doubles(int m, int n, int K) {
-    int mn = m < n ? m : n;
-    return (long)m * n + 3L * K + (long)kCacheCap * (3 + 4 + 12) + mn + 16 + (long)kSolCap * (n + 1);
-}
 
 struct Warp {
     const Params *P;

@@ -60,7 +60,7 @@ class MockOptsC(C.Structure):
 # Every symbol include/decaes_gpu.h declares.
 EXPORTS = ["decaes_create", "decaes_destroy", "decaes_last_error", "decaes_get_stats", "decaes_t2map_check_options",
            "decaes_t2part_check_options", "decaes_t2map", "decaes_t2part", "decaes_t2map_t2part",
-           "decaes_t2map_t2part_device", "decaes_sync_stats", "decaes_mock_image"]
+           "decaes_t2map_t2part_device", "decaes_sync_stats", "decaes_mock_image", "decaes_t2map_t2part_noalloc"]
 
 _lib = None
 
@@ -96,6 +96,8 @@ def load(build_if_needed: bool = True):
                                              C.POINTER(T2mapOutC), C.POINTER(T2partOutC), _vp]
     L.decaes_sync_stats.argtypes = [_vp, _vp]
     L.decaes_mock_image.argtypes = [C.POINTER(MockOptsC), C.c_uint64, _vp, C.c_int, C.c_int]
+    L.decaes_t2map_t2part_noalloc.argtypes = [C.POINTER(T2mapOptsC), C.POINTER(T2partOptsC), _vp, C.c_int, _vp,
+                                              C.POINTER(T2mapOutC), C.POINTER(T2partOutC), _vp, C.c_char_p, C.c_size_t]
     _lib = L
     return L
 

@@ -40,7 +40,8 @@ enum {
     DECAES_OK = 0,
     DECAES_EINVAL = 1,   /* invalid option or argument (reference AssertionError) */
     DECAES_ECUDA = 2,    /* CUDA runtime error */
-    DECAES_ENOMEM = 3,   /* allocation would exceed the context's HBM budget */
+    DECAES_ENOMEM = 3,   /* allocation would exceed the context's HBM budget, or the
+                            problem does not fit the no-allocation workspace */
     DECAES_ELEGACY = 4,  /* legacy=true algorithms are not provided */
 };
 
@@ -154,6 +155,46 @@ int decaes_t2map_t2part_device(decaes_ctx *ctx, const decaes_t2map_opts *mopts, 
 /* Waits for the last device-pointer call on `stream` and completes its
  * decaes_stats (processed voxels, cap hits, device times). */
 int decaes_sync_stats(decaes_ctx *ctx, void *stream);
+
+/* Fused T2mapSEcorr + T2partSEcorr that allocates no device memory.  This entry
+ * point has no counterpart in the reference; it exists for callers that cannot
+ * let a library allocate: a host with a fixed device-memory plan (a real-time
+ * reconstruction pipeline, an embedding runtime whose allocator is the only
+ * one allowed) or code running where cudaMalloc is not permitted.  It needs no
+ * decaes_ctx.
+ *
+ * All pointers are device addresses on the CURRENT device; `stream` is a
+ * cudaStream_t (NULL = the legacy default stream).  `d_image` (and the optional
+ * `d_b1map`) are DECAES_F32 or DECAES_F64 per `dtype`; every output is FP64
+ * whatever `dtype` is.  dist, gdn, ggm, gva, fnr, snr and alpha are required;
+ * resnorm, decaycurve, mu, chi2factor and decaybasis are written when non-NULL;
+ * echotimes, t2times, refangleset and decaybasisset must be NULL.  T2part is
+ * fused when `popts` and `d_pout` are given (both or neither).  The library
+ * NaN-fills the outputs before the solve.  Returns before the work finishes:
+ * synchronize `stream` before reading the outputs.  Error text goes to
+ * `err` (`errlen` bytes, may be NULL).
+ *
+ * Working memory is one static device array of DECAES_NOALLOC_SCRATCH_BYTES
+ * (64 MiB) per device, reserved when the CUDA module holding it is loaded (at
+ * the first call under CUDA's default lazy module loading).
+ * It holds the counters, grids, angle-ensemble basis (8*nTE*nT2*nRefAngles*2
+ * bytes), the foreground voxel list (4 bytes per voxel) and the per-warp solver
+ * scratch; a problem whose fixed part leaves no room for one warp's scratch is
+ * rejected with DECAES_ENOMEM (split the image into slabs: voxels are
+ * independent).  Fewer resident warps fit when the voxel list is large, which
+ * lowers throughput but not the results, which are bit-identical to
+ * decaes_t2map_t2part_device.
+ *
+ * The first call on each device does a one-time set-up (symbol lookup of the
+ * array, device attributes); make that first call before any stream capture.
+ * All calls on a device share the array and it keeps the last call's contents:
+ * calls that overlap in time on one device -- from two host threads or on two
+ * streams -- race on it and give undefined results.  Serialize them. */
+#define DECAES_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
+int decaes_t2map_t2part_noalloc(const decaes_t2map_opts *mopts, const decaes_t2part_opts *popts,
+                                const void *d_image, int dtype, const void *d_b1map,
+                                const decaes_t2map_out *d_mout, const decaes_t2part_out *d_pout,
+                                void *stream, char *err, size_t errlen);
 
 /* Synthetic multi-echo image, the counterpart of mock_image
  * (src/utils.jl:606-668) with the generator used by this project's benchmarks:
