@@ -64,6 +64,25 @@ __global__ void k_basis_fixed(int m, int n, double alpha, double TE, double T1, 
     }
 }
 
+// Gram matrices G_k = A_k'A_k of the K grid bases (mixed method), one block
+// per basis, threads over the upper-triangle entries.
+__global__ void k_gram_grid(int m, int n, const double *As, double *Gs) {
+    const int k = blockIdx.x;
+    const double *A = As + (long)k * m * n;
+    double *G = Gs + (long)k * n * n;
+    const int npairs = n * (n + 1) / 2;
+    for (int p = threadIdx.x; p < npairs; p += blockDim.x) {
+        int j = 0;
+        while ((j + 1) * (j + 2) / 2 <= p) ++j;
+        int i = p - j * (j + 1) / 2;
+        const double *ai = A + (long)i * m, *aj = A + (long)j * m;
+        double s = 0.0;
+        for (int r = 0; r < m; ++r) s = fma(ai[r], aj[r], s);
+        G[i + (long)n * j] = s;
+        G[j + (long)n * i] = s;
+    }
+}
+
 __global__ void k_fill(double *p, long len, double v) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < len; i += (long)gridDim.x * blockDim.x) p[i] = v;
 }
@@ -86,6 +105,7 @@ __global__ void k_compact(const void *image, int f32, long V, double thr, int *v
 }
 
 // Persistent voxel solver: one warp per voxel, voxels pulled from a counter.
+// P.mixed selects the method (warp-uniform for the whole launch).
 __global__ void __launch_bounds__(32) k_voxels(const __grid_constant__ Params P) {
     extern __shared__ double smem[];
     Warp w;
@@ -93,22 +113,52 @@ __global__ void __launch_bounds__(32) k_voxels(const __grid_constant__ Params P)
     w.lane = threadIdx.x & 31;
     w.nnls_caps = 0;
     w.loop_caps = 0;
+    w.mixed = P.mixed != 0;
     const int n = P.n, lda = P.lda;
     double *p = smem;
-    w.s.C = p; p += (long)lda * n;
-    w.s.b = p; p += lda;
-    w.s.zz = p; p += lda;
-    w.data = p; p += lda;
-    w.s.x = p; p += n;
-    w.s.w = p; p += n;
-    w.xout = p; p += n;
-    w.s.rdiag = p; p += n;
-    p += 8;
-    w.s.idx = reinterpret_cast<int *>(p);
-    w.s.posof = w.s.idx + n;
-    w.s.zl = w.s.posof + n;
-    w.s.diag = reinterpret_cast<unsigned char *>(w.s.zl + 2 * n);
-    w.s.lda = lda;
+    if (w.mixed) {
+        // normal-equation workspace (see warp_smem_doubles_mixed)
+        const int m = P.m;
+        w.data = p; p += m;
+        w.s.x = p; p += n;
+        w.s.w = p; p += n;
+        w.xout = p; p += n;
+        w.g.G = p; p += mixed_r1_doubles(m, n);
+        w.g.L = p; p += mixed_r2_doubles(m, n);
+        w.g.f = p; p += n;
+        w.g.y = p; p += n;
+        w.g.rinv = p; p += n;
+        w.g.xp = p; p += n;
+        p += 8;
+        int *ip = reinterpret_cast<int *>(p);
+        w.s.idx = ip;
+        w.g.P = ip + n;
+        w.g.pos = ip + 2 * n;
+        w.g.lastP = ip + 3 * n;
+        w.g.S = n | 1;
+        w.g.lastk = 0;
+        w.As = w.g.L;  // the staged basis is consumed before the first factorization
+        w.ldA = m | 1;
+        w.s.C = w.g.L;  // GCV singular-value workspace
+        w.s.zz = w.g.y;
+        w.s.b = nullptr; w.s.rdiag = nullptr; w.s.posof = nullptr; w.s.zl = nullptr; w.s.diag = nullptr;
+        w.s.lda = lda;
+    } else {
+        w.s.C = p; p += (long)lda * n;
+        w.s.b = p; p += lda;
+        w.s.zz = p; p += lda;
+        w.data = p; p += lda;
+        w.s.x = p; p += n;
+        w.s.w = p; p += n;
+        w.xout = p; p += n;
+        w.s.rdiag = p; p += n;
+        p += 8;
+        w.s.idx = reinterpret_cast<int *>(p);
+        w.s.posof = w.s.idx + n;
+        w.s.zl = w.s.posof + n;
+        w.s.diag = reinterpret_cast<unsigned char *>(w.s.zl + 2 * n);
+        w.s.lda = lda;
+    }
     w.scr = P.scratch + (long)blockIdx.x * P.scr_stride;
     {
         const int mn = P.m < P.n ? P.m : P.n;
@@ -192,6 +242,7 @@ struct BasisKey {
 };
 struct Basis {
     double *t2 = nullptr, *logt2 = nullptr, *angles = nullptr, *As = nullptr, *dAs = nullptr, *fixed = nullptr;
+    double *Gs = nullptr;  // Gram matrices of the grid (or fixed) bases, made on first use by the mixed method
     std::vector<double> h_t2, h_angles;
     size_t bytes = 0;
     long last_use = 0;
@@ -262,6 +313,7 @@ int get_basis(decaes_ctx *ctx, const decaes_t2map_opts &o, Basis **out) {
             if (i->second.last_use < lru->second.last_use) lru = i;
         Basis &b = lru->second;
         cudaFree(b.t2); cudaFree(b.logt2); cudaFree(b.angles); cudaFree(b.As); cudaFree(b.dAs); cudaFree(b.fixed);
+        cudaFree(b.Gs);
         ctx->used -= b.bytes;
         ctx->bases.erase(lru);
     }
@@ -318,9 +370,23 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
     if (n > 256) return fail(ctx, DECAES_EINVAL, "nT2 > 256 is not supported by this build");
     const bool fixed = !std::isnan(o.SetFlipAngle);
     if (!fixed && o.nRefAngles > 256) return fail(ctx, DECAES_EINVAL, "nRefAngles > 256 is not supported by this build");
+    const bool mixed = o.precision == DECAES_PREC_MIXED;
+    if (mixed && n > dk::kGramMaxN)
+        return fail(ctx, DECAES_EINVAL, "precision = mixed supports nT2 <= " + std::to_string(dk::kGramMaxN));
     Basis *B;
     if (int rc = get_basis(ctx, o, &B)) return rc;
     int nl = 0;
+    if (mixed && !B->Gs) {
+        const int K = fixed ? 1 : o.nRefAngles;
+        const size_t gb = sizeof(double) * (size_t)K * n * n;
+        if (ctx->used + gb > ctx->budget) return fail(ctx, DECAES_ENOMEM, "Gram matrices exceed the HBM budget");
+        CK(cudaMalloc(&B->Gs, gb));
+        B->bytes += gb;
+        ctx->used += gb;
+        dk::k_gram_grid<<<K, 256, 0, st>>>(m, n, fixed ? B->fixed : B->As, B->Gs);
+        ++nl;
+        CK(cudaGetLastError());
+    }
     // T2part plan (fused)
     dh::T2partPlan pp{};
     double *d_weights = nullptr;
@@ -372,15 +438,21 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
         P.fuse_t2part = 1; P.sp0 = pp.sp0; P.sp1 = pp.sp1; P.mp0 = pp.mp0; P.mp1 = pp.mp1; P.weights = d_weights;
         P.sfr = out.sfr; P.sgm = out.sgm; P.mfr = out.mfr; P.mgm = out.mgm;
     }
-    long wsm = dk::warp_smem_doubles(m, n, P.lda);
+    if (mixed) {
+        P.mixed = 1;
+        P.Gs = B->Gs;
+        P.epg_lanes_f32 = (int)std::min<long>(32, 2 * dk::mixed_r1_doubles(m, n) / (3L * m));
+    }
+    long wsm = mixed ? dk::warp_smem_doubles_mixed(m, n) : dk::warp_smem_doubles(m, n, P.lda);
     size_t smem = (size_t)wsm * sizeof(double);
     if (smem > ctx->smem_optin)
         return fail(ctx, DECAES_EINVAL, "nTE/nT2 too large: the per-voxel workspace (" + std::to_string(smem) +
                                             " bytes) exceeds shared memory per block");
     P.epg_lanes = (int)std::min<long>(32, ((long)P.lda * n) / (3L * m));
-    CK(cudaFuncSetAttribute(dk::k_voxels, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    auto kern = dk::k_voxels;
+    CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dk::k_voxels, 32, smem));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem));
     if (per_sm < 1) return fail(ctx, DECAES_EINVAL, "voxel kernel cannot be resident with this workspace size");
     const int grid = per_sm * ctx->sms;
     P.scr_stride = dk::warp_scratch_doubles(m, n, P.K);
@@ -388,7 +460,7 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
     if (int rc = buf(ctx, "scratch", sizeof(double) * (size_t)P.scr_stride * grid, &scr)) return rc;
     P.scratch = (double *)scr;
     cudaEventRecord(ctx->ev[2], st);
-    dk::k_voxels<<<grid, 32, smem, st>>>(P);
+    kern<<<grid, 32, smem, st>>>(P);
     cudaEventRecord(ctx->ev[3], st);
     ++nl;
     CK(cudaGetLastError());
@@ -511,6 +583,7 @@ extern "C" void decaes_destroy(decaes_ctx *ctx) {
     for (auto &kv : ctx->bases) {
         Basis &b = kv.second;
         cudaFree(b.t2); cudaFree(b.logt2); cudaFree(b.angles); cudaFree(b.As); cudaFree(b.dAs); cudaFree(b.fixed);
+        cudaFree(b.Gs);
     }
     for (auto &e : ctx->ev) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);

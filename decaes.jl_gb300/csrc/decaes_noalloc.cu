@@ -142,6 +142,8 @@ extern "C" int decaes_t2map_t2part_noalloc(const decaes_t2map_opts *mopts, const
     if (d_pout && (!d_pout->sfr || !d_pout->sgm || !d_pout->mfr || !d_pout->mgm))
         return fail(err, errlen, DECAES_EINVAL, "sfr, sgm, mfr and mgm outputs are required with T2part options");
 
+    if (o.precision != DECAES_PREC_FP64)
+        return fail(err, errlen, DECAES_EINVAL, "this entry point runs the FP64 method only (precision = DECAES_PREC_FP64)");
     const int m = o.nTE, n = o.nT2;
     const bool fixed = !std::isnan(o.SetFlipAngle);
     const int K = fixed ? 1 : o.nRefAngles;

@@ -61,6 +61,10 @@ DX_HD Dual absd(Dual a) { return signbit(a.v) ? -a : a; }
 DX_HD double absd(double a) { return fabs(a); }
 DX_HD double zero_of(double) { return 0.0; }
 DX_HD Dual zero_of(Dual) { return Dual{0.0, 0.0}; }
+// single-precision recursion of the mixed method
+DX_HD float fmad(float a, float b, float c) { return fmaf(a, b, c); }
+DX_HD float absd(float a) { return fabsf(a); }
+DX_HD float zero_of(float) { return 0.0f; }
 
 // sind: the degree reduction of Base.sind with a double-double radian
 // argument (sin(h + l) = sin h + l cos h to first order).
@@ -124,6 +128,12 @@ DX_HD FlatCoef<Dual> flat_coef_dual(double alpha_deg, double TE, double T2, doub
     return k;
 }
 
+// Coefficients rounded to single precision (mixed method; the coefficients
+// themselves are evaluated in FP64).
+DX_HD FlatCoef<float> to_f32(const FlatCoef<double> &k) {
+    return FlatCoef<float>{(float)k.a, (float)k.b, (float)k.c, (float)k.d, (float)k.cp, (float)k.m0};
+}
+
 // One state of the constant-flip step: outputs (F of state k+1, Fbar of
 // state k-1, Z of state k) from (F, Fbar, Z) of state k.
 template <class T>
@@ -136,8 +146,8 @@ DX_HD void flat_state(const FlatCoef<T> &q, T F, T Fb, T Z, T &oF, T &oFb, T &oZ
 
 // epg_decay_curve! for the constant-flip kernel: impulse response, then
 // dc[i] = |m0 * dc[i]|.  S holds 3*ETL strided values (st apart).
-template <class T>
-DX_HD void epg_flat_inplace(int ETL, const FlatCoef<T> &q, T *S, int st, T *dc, int dst) {
+template <class T, class O>
+DX_HD void epg_flat_inplace(int ETL, const FlatCoef<T> &q, T *S, int st, O *dc, int dst) {
 #define EF(k) S[((k)-1) * st]
 #define EFb(k) S[(ETL + (k)-1) * st]
 #define EZ(k) S[(2 * ETL + (k)-1) * st]
@@ -230,10 +240,17 @@ DX_HD VecCoef<Dual> vec_coef_dual(double alpha_deg, double TE, double T2, double
     return k;
 }
 
+DX_HD VecCoef<float> to_f32(const VecCoef<double> &k) {
+    VecCoef<float> o;
+    for (int c = 0; c < 3; ++c) { o.F[c] = (float)k.F[c]; o.Fb[c] = (float)k.Fb[c]; o.Z[c] = (float)k.Z[c]; }
+    o.a1 = (float)k.a1; o.b1 = (float)k.b1; o.c1 = (float)k.c1; o.m0 = (float)k.m0;
+    return o;
+}
+
 // epg_decay_curve! for EPGOptions (DualVector_Split_Dynamic), in place.
 // S holds 3*ETL strided values: state k's (x,y,z) at S[(3(k-1)+c)*st].
-template <class T>
-DX_HD void epg_vec_inplace(int ETL, const VecCoef<T> &q, T *S, int st, T *dc, int dst) {
+template <class T, class O>
+DX_HD void epg_vec_inplace(int ETL, const VecCoef<T> &q, T *S, int st, O *dc, int dst) {
 #define SX(k, c) S[(3 * ((k)-1) + (c)) * st]
     const T z0 = zero_of(q.m0);
     T M0x = q.b1 * q.m0, M0z = ((-q.c1) * q.m0) / 2;

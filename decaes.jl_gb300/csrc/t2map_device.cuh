@@ -4,6 +4,7 @@
 // src/lsqnonneg.jl; src/splines.jl; src/optimization.jl; src/T2partSEcorr.jl).
 #pragma once
 #include "epg.cuh"
+#include "nnls_gram.cuh"
 #include "nnls_warp.cuh"
 #include "t2map_params.cuh"
 
@@ -20,9 +21,35 @@ struct Warp {
     int nsol;
     int lane;
     unsigned nnls_caps, loop_caps;
+    // mixed method: normal-equation workspace and the staged basis (shared)
+    GramWS g;
+    double *As;    // basis staged in shared memory, column-major, leading dimension ldA
+    int ldA;
+    bool mixed;    // the mixed method (Params::mixed)
 };
 
 __device__ __forceinline__ void note(Warp &w, const NnlsResult &r) { w.nnls_caps += (r.mode != 0); }
+
+// Copies an m x n column-major basis from global memory to w.As (leading
+// dimension ldA), coalesced.
+__device__ void stage_basis(Warp &w, const double *A) {
+    const int m = w.P->m, n = w.P->n;
+    for (long q = w.lane; q < (long)m * n; q += 32) {
+        const int i = (int)(q % m), j = (int)(q / m);
+        w.As[i + (long)w.ldA * j] = A[q];
+    }
+    __syncwarp();
+}
+
+// Unregularized (tikh = false) or Tikhonov solve on the voxel's basis w.A:
+// the reference's Householder NNLS for the plain method, the normal-equation
+// solver on the voxel's prepared Gram matrix for the mixed method.
+__device__ NnlsResult basis_lsq(Warp &w, bool tikh, double mu) {
+    const Params &P = *w.P;
+    if (w.mixed)
+        return gram_nnls(w.g, w.s.x, w.s.w, w.s.idx, w.A, P.m, P.n, w.data, tikh ? mu * mu : 0.0, 3 * P.n, &w.g.lastk);
+    return warp_lsq(w.s, w.A, P.m, P.n, w.data, tikh, mu);
+}
 
 // Keys with Julia's isless order (NaN above everything, -0.0 < +0.0), for
 // findmax-style searches on the integer pipes.
@@ -81,7 +108,7 @@ struct TikhState {
 };
 __device__ TikhState tikh_solve(Warp &w, double mu) {
     TikhState t;
-    t.r = warp_lsq(w.s, w.A, w.P->m, w.P->n, w.data, true, mu);
+    t.r = basis_lsq(w, true, mu);
     t.mu = mu;
     note(w, t.r);
     return t;
@@ -257,7 +284,7 @@ struct MdpF {  // f(logμ) of lsqnonneg_mdp!, src/lsqnonneg.jl:723-726
 // reference saves its smoothing cache's stale slot; x_unreg is stored here.
 __device__ void reg_chi2(Warp &w, double chi2_target, double &mu_out, double &chi2_out) {
     const Params &P = *w.P;
-    NnlsResult r0 = warp_lsq(w.s, w.A, P.m, P.n, w.data, false, 0.0);
+    NnlsResult r0 = basis_lsq(w, false, 0.0);
     note(w, r0);
     double res2_min = __dmul_rn(r0.rnorm, r0.rnorm);
     if (res2_min == 0 || r0.nsetp == 0) {
@@ -293,7 +320,7 @@ __device__ void reg_chi2(Warp &w, double chi2_target, double &mu_out, double &ch
 // x (x_unreg or zeros) where the reference saves a stale cache slot.
 __device__ void reg_mdp(Warp &w, double delta, double &mu_out, double &chi2_out) {
     const Params &P = *w.P;
-    NnlsResult r0 = warp_lsq(w.s, w.A, P.m, P.n, w.data, false, 0.0);
+    NnlsResult r0 = basis_lsq(w, false, 0.0);
     note(w, r0);
     double res2_min = __dmul_rn(r0.rnorm, r0.rnorm);
     if (delta <= sqrt(res2_min)) { save_x(w); mu_out = 0; chi2_out = 1; return; }
@@ -543,7 +570,7 @@ __device__ void reg_lcurve(Warp &w, double &mu_out, double &chi2_out) {
         TikhState t = tikh_solve(w, mu);
         double res2 = tikh_res2(w, t);
         save_x(w);
-        NnlsResult r0 = warp_lsq(w.s, w.A, w.P->m, w.P->n, w.data, false, 0.0);
+        NnlsResult r0 = basis_lsq(w, false, 0.0);
         note(w, r0);
         chi2 = res2 / __dmul_rn(r0.rnorm, r0.rnorm);
     } else {
@@ -631,7 +658,7 @@ struct GcvF {  // log𝒢(logμ), src/lsqnonneg.jl:1150-1154 and gcv!, 1213-1229
 __device__ void reg_gcv(Warp &w, double &mu_out, double &chi2_out) {
     const Params &P = *w.P;
     double *gam = w.scr + (long)P.m * P.n + 3L * P.K + (long)kCacheCap * 19;
-    warp_svdvals(w, gam);
+    if (!w.mixed) warp_svdvals(w, gam);  // the mixed method computes them before its Gram matrix overwrites the workspace
     GcvF f{&w, gam, (2.220446049250313e-16 * 2.220446049250313e-16) / P.m};
     double logmu, logG;
     brent_minimize(f, -8.0, 2.0, 0.0, 1e-4, 20, logmu, logG);
@@ -641,7 +668,7 @@ __device__ void reg_gcv(Warp &w, double &mu_out, double &chi2_out) {
         TikhState t = tikh_solve(w, mu);
         double res2 = tikh_res2(w, t);
         save_x(w);
-        NnlsResult r0 = warp_lsq(w.s, w.A, P.m, P.n, w.data, false, 0.0);
+        NnlsResult r0 = basis_lsq(w, false, 0.0);
         note(w, r0);
         chi2 = res2 / __dmul_rn(r0.rnorm, r0.rnorm);
     } else {
@@ -670,7 +697,16 @@ __device__ void fa_update(Search &S, int I) {
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lane = w.lane;
     const double *A = P.As + (long)(I - 1) * m * n, *dA = P.dAs + (long)(I - 1) * m * n;
-    NnlsResult r = warp_lsq(w.s, A, m, n, w.data, false, 0.0);
+    NnlsResult r;
+    if (w.mixed) {
+        // precomputed Gram matrix of grid basis I; A'b from the basis staged in shared memory
+        gram_load(w.g, P.Gs + (long)(I - 1) * n * n, n);
+        stage_basis(w, A);
+        gram_rhs(w.g, w.As, w.ldA, m, n, w.data);
+        r = gram_nnls(w.g, w.s.x, w.s.w, w.s.idx, A, m, n, w.data, 0.0, 3 * n, &w.g.lastk);
+    } else {
+        r = warp_lsq(w.s, A, m, n, w.data, false, 0.0);
+    }
     note(w, r);
     double ell = __dmul_rn(r.rnorm, r.rnorm);
     double part = 0;
@@ -858,6 +894,35 @@ __device__ void warp_basis(Warp &w, double alpha, double *out /* m x n, global *
     __syncwarp();
 }
 
+// Mixed method: the same curves with the recursion in FP32 (coefficients in
+// FP64, rounded once), states in the Gram region, written to w.As and then
+// copied to w.A (global) for the fitted curve and the explicit residuals.
+__device__ void warp_basis_f32(Warp &w, double alpha) {
+    const Params &P = *w.P;
+    const int m = P.m, n = P.n, lanes = P.epg_lanes_f32, lane = w.lane;
+    float *S = reinterpret_cast<float *>(w.g.G);  // 3*m*lanes floats, lane-contiguous
+    for (int j0 = 0; j0 < n; j0 += lanes) {
+        int j = j0 + lane;
+        if (lane < lanes && j < n) {
+            float *Sl = S + lane;
+            if (P.beta180) {
+                dx::FlatCoef<float> q = dx::to_f32(dx::flat_coef(alpha, P.TE, P.t2[j], P.T1));
+                dx::epg_flat_inplace(m, q, Sl, lanes, w.As + (long)j * w.ldA, 1);
+            } else {
+                dx::VecCoef<float> q = dx::to_f32(dx::vec_coef(alpha, P.TE, P.t2[j], P.T1, P.beta));
+                dx::epg_vec_inplace(m, q, Sl, lanes, w.As + (long)j * w.ldA, 1);
+            }
+        }
+        __syncwarp();
+    }
+    for (long q = lane; q < (long)m * n; q += 32) {
+        const int i = (int)(q % m), j = (int)(q / m);
+        w.A[q] = w.As[i + (long)w.ldA * j];
+    }
+    __threadfence_block();
+    __syncwarp();
+}
+
 // ----------------------------------------------------------------------------
 // One voxel (src/T2mapSEcorr.jl:201-238, save_results! 512-591, T2part 95-138)
 // ----------------------------------------------------------------------------
@@ -884,9 +949,11 @@ __device__ void process_voxel(Warp &w, long v) {
     __syncwarp();
 
     double alpha;
+    w.g.lastk = 0;  // warm starts never cross voxels (results independent of scheduling)
     if (P.angle_mode == 1) {
         alpha = P.fixed_angle;
         w.A = const_cast<double *>(P.basis_fixed);
+        if (w.mixed) stage_basis(w, w.A);
     } else {
         w.A = w.scr;
         if (P.angle_mode == 2) {
@@ -894,13 +961,23 @@ __device__ void process_voxel(Warp &w, long v) {
         } else {
             alpha = flip_angle_search(w);
         }
-        warp_basis(w, alpha, w.A);
+        if (w.mixed) warp_basis_f32(w, alpha);
+        else warp_basis(w, alpha, w.A);
+    }
+    if (w.mixed) {
+        // Gram matrix and right-hand side of the voxel's basis, shared by every
+        // solve of the regularizer; GCV's singular values first (their
+        // workspace overlaps the staged basis, not the Gram matrix)
+        if (P.angle_mode == 1) gram_load(w.g, P.Gs, n);
+        else gram_build(w.g, w.As, w.ldA, m, n);
+        gram_rhs(w.g, w.As, w.ldA, m, n, w.data);
+        if (P.reg == 2) warp_svdvals(w, w.scr + (long)P.m * P.n + 3L * P.K + (long)kCacheCap * 19);
     }
 
     double mu = CUDART_NAN, chi2 = CUDART_NAN;
     switch (P.reg) {
     case 0: {  // none
-        NnlsResult r = warp_lsq(w.s, w.A, m, n, w.data, false, 0.0);
+        NnlsResult r = basis_lsq(w, false, 0.0);
         note(w, r);
         save_x(w);
         mu = 0; chi2 = 1;

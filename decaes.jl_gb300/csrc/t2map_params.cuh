@@ -34,6 +34,10 @@ struct Params {
     double *sfr, *sgm, *mfr, *mgm;
     int need_chi2;
     int epg_lanes;
+    // mixed-precision method (normal-equation NNLS, FP32 EPG at the fitted angle)
+    int mixed;
+    const double *Gs;   // Gram matrices A_k'A_k of the grid bases (K x n x n), or of the fixed basis
+    int epg_lanes_f32;  // lanes of the FP32 EPG (states in the Gram region)
 };
 
 // Shared-memory footprint of one warp worker (doubles), mirrored on the host.
@@ -42,6 +46,25 @@ __host__ __device__ inline long warp_smem_doubles(int m, int n, int lda) {
     long ints = 4L * n;            // idx, posof, zl
     long bytes = (long)n;          // diag
     return d + (ints * 4 + bytes + 7) / 8;
+}
+// Shared-memory regions of one warp worker of the mixed method (doubles):
+// R1 holds the Gram matrix (and the FP32 EPG states before it is built), R2
+// the Cholesky factor, the staged basis and the GCV singular-value workspace.
+__host__ __device__ inline long mixed_r1_doubles(int m, int n) {
+    long a = (long)n * (n | 1), b = 3L * m;
+    return a > b ? a : b;
+}
+__host__ __device__ inline long mixed_r2_doubles(int m, int n) {
+    long a = (long)n * (n | 1), b = (long)(m | 1) * n;
+    int r = m >= n ? m : n, c = m >= n ? n : m;
+    long u = (long)(r | 1) * c;
+    long x = a > b ? a : b;
+    return x > u ? x : u;
+}
+__host__ __device__ inline long warp_smem_doubles_mixed(int m, int n) {
+    long d = (long)m + 3L * n + mixed_r1_doubles(m, n) + mixed_r2_doubles(m, n) + 4L * n + 8;
+    long ints = 4L * n;  // idx, P, pos, lastP
+    return d + (ints * 4 + 7) / 8;
 }
 // Global scratch of one warp worker (doubles).
 __host__ __device__ inline long warp_scratch_doubles(int m, int n, int K) {

@@ -1,0 +1,87 @@
+"""The mixed-precision method (DECAES_PREC_MIXED) against the FP64 oracle.
+
+The mixed method solves the same problems with a different algorithm
+(normal-equation Lawson-Hanson with warm starts, FP32 EPG at the fitted angle),
+so it is not bit-exact; its errors against the FP64 oracle are stated per
+output and held to:
+  MWF (sfr)            max |d| <= 1e-3 (the accuracy gate of the method)
+  distribution L1      relative, p99 <= 1e-3
+  flip angle           max |d| <= 1e-2 degrees
+"""
+import numpy as np
+import pytest
+
+from parity import orc_opts
+
+pytestmark = pytest.mark.gpu
+
+SPWIN, MPWIN = (10e-3, 25e-3), (25e-3, 200e-3)
+MWF_GATE = 1e-3
+DIST_L1_P99 = 1e-3
+ALPHA_ATOL = 1e-2
+
+CASES = {
+    "lcurve48": dict(X=(24, 20, 2), m=48, TE=10e-3, n=40, T2=(10e-3, 2.0), K=32, Reg="lcurve", bg=0.35, thr=200.0),
+    "gcv56": dict(X=(16, 12, 2), m=56, TE=7e-3, n=60, T2=(8e-3, 2.0), K=64, Reg="gcv"),
+    "chi2": dict(X=(16, 16, 2), m=32, TE=10e-3, n=40, T2=(10e-3, 2.0), K=8, Reg="chi2", Chi2Factor=1.02),
+    "none": dict(X=(16, 16, 1), m=48, TE=10e-3, n=40, T2=(10e-3, 2.0), K=16, Reg="none"),
+    "mdp": dict(X=(16, 16, 1), m=48, TE=10e-3, n=40, T2=(10e-3, 2.0), K=16, Reg="mdp", NoiseLevel=2.0),
+    "refcon150": dict(X=(12, 12, 1), m=32, TE=10e-3, n=40, T2=(10e-3, 2.0), K=16, Reg="lcurve", RefConAngle=150.0),
+    "fixed_angle": dict(X=(16, 16, 1), m=48, TE=10e-3, n=40, T2=(10e-3, 2.0), K=16, Reg="lcurve", SetFlipAngle=165.0),
+    "m_lt_n": dict(X=(12, 12, 1), m=24, TE=10e-3, n=48, T2=(10e-3, 2.0), K=8, Reg="gcv"),
+}
+
+
+def mixed_vs_oracle(D, orc, ctx, c, seed=21):
+    img = D.mock_image(D.MockImageOptions(MatrixSize=c["X"], nTE=c["m"], TE=c["TE"],
+                                          BackgroundFraction=c.get("bg", 0.0)), seed=seed)
+    kw = dict(MatrixSize=c["X"], nTE=c["m"], TE=c["TE"], nT2=c["n"], T2Range=c["T2"], Reg=c["Reg"],
+              nRefAngles=c["K"], Chi2Factor=c.get("Chi2Factor"), NoiseLevel=c.get("NoiseLevel"),
+              Threshold=c.get("thr", 0.0), RefConAngle=c.get("RefConAngle", 180.0),
+              SetFlipAngle=c.get("SetFlipAngle"), SaveRegParam=True, SaveResidualNorm=True)
+    o = D.T2mapOptions(**kw, precision="mixed")
+    po = D.T2partOptions.from_t2map(o, SPWin=SPWIN, MPWin=MPWIN)
+    maps, dist, parts = D.T2mapSEcorr_T2partSEcorr(img, o, po, ctx=ctx)
+    om, od = orc.t2map(img, orc_opts(orc, D.T2mapOptions(**kw)), nthreads=8)
+    op = orc.t2part(od, orc.T2partOptions(MatrixSize=c["X"], nT2=c["n"], T2Range=c["T2"], SPWin=SPWIN, MPWin=MPWIN))
+    return maps, dist, parts, om, od, op
+
+
+def errors(c, maps, dist, parts, om, od, op):
+    n = c["n"]
+    a, b = dist.reshape(-1, n), od.reshape(-1, n)
+    ok = ~np.isnan(b).any(axis=1)
+    l1 = np.abs(a[ok] - b[ok]).sum(1) / np.maximum(np.abs(b[ok]).sum(1), 1e-300)
+    mwf = np.abs(parts["sfr"] - op["sfr"]).ravel()
+    mwf = mwf[~np.isnan(mwf)]
+    da = np.abs(maps["alpha"] - om["alpha"]).ravel()
+    da = da[~np.isnan(da)]
+    return dict(voxels=int(ok.sum()), mwf_max=float(mwf.max()), mwf_p99=float(np.quantile(mwf, 0.99)),
+                l1_p99=float(np.quantile(l1, 0.99)), l1_max=float(l1.max()), alpha_max=float(da.max()))
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_mixed_within_gate(D, orc, ctx, name):
+    c = CASES[name]
+    maps, dist, parts, om, od, op = mixed_vs_oracle(D, orc, ctx, c)
+    # same voxels processed, same NaN pattern
+    np.testing.assert_array_equal(np.isnan(dist), np.isnan(od))
+    np.testing.assert_array_equal(np.isnan(parts["sfr"]), np.isnan(op["sfr"]))
+    e = errors(c, maps, dist, parts, om, od, op)
+    print(f"{name}: {e}")
+    assert e["mwf_max"] <= MWF_GATE
+    assert e["l1_p99"] <= DIST_L1_P99
+    assert e["alpha_max"] <= ALPHA_ATOL
+
+
+def test_mixed_deterministic(D, ctx):
+    """Warm starts never cross voxels, so results do not depend on which warp
+    processed which voxel: two runs are bitwise equal."""
+    c = CASES["lcurve48"]
+    img = D.mock_image(D.MockImageOptions(MatrixSize=c["X"], nTE=c["m"], TE=c["TE"], BackgroundFraction=0.35), seed=3)
+    o = D.T2mapOptions(MatrixSize=c["X"], nTE=c["m"], TE=c["TE"], nT2=c["n"], T2Range=c["T2"], Reg="lcurve",
+                       nRefAngles=c["K"], Threshold=200.0, precision="mixed")
+    m1, d1 = D.T2mapSEcorr(img, o, ctx=ctx)
+    m2, d2 = D.T2mapSEcorr(img, o, ctx=ctx)
+    np.testing.assert_array_equal(d1, d2)
+    np.testing.assert_array_equal(m1["alpha"], m2["alpha"])
