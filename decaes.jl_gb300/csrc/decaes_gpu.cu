@@ -64,12 +64,14 @@ __global__ void k_basis_fixed(int m, int n, double alpha, double TE, double T1, 
     }
 }
 
-// Gram matrices G_k = A_k'A_k of the K grid bases (mixed method), one block
-// per basis, threads over the upper-triangle entries.
-__global__ void k_gram_grid(int m, int n, const double *As, double *Gs) {
+// Mixed method, once per basis key: packed Gram matrices G_k = A_k'A_k of
+// the K grid bases (upper triangle by columns) and the bases transposed to
+// row-major, one block per basis.
+__global__ void k_gram_grid(int m, int n, const double *As, double *Gs, double *AsT) {
     const int k = blockIdx.x;
     const double *A = As + (long)k * m * n;
-    double *G = Gs + (long)k * n * n;
+    double *G = Gs + (long)k * (n * (n + 1) / 2);
+    double *AT = AsT + (long)k * m * n;
     const int npairs = n * (n + 1) / 2;
     for (int p = threadIdx.x; p < npairs; p += blockDim.x) {
         int j = 0;
@@ -78,8 +80,11 @@ __global__ void k_gram_grid(int m, int n, const double *As, double *Gs) {
         const double *ai = A + (long)i * m, *aj = A + (long)j * m;
         double s = 0.0;
         for (int r = 0; r < m; ++r) s = fma(ai[r], aj[r], s);
-        G[i + (long)n * j] = s;
-        G[j + (long)n * i] = s;
+        G[p] = s;
+    }
+    for (int q = threadIdx.x; q < m * n; q += blockDim.x) {
+        const int i = q / n, j = q % n;
+        AT[q] = A[i + (long)m * j];
     }
 }
 
@@ -124,10 +129,11 @@ __global__ void __launch_bounds__(32) k_voxels(const __grid_constant__ Params P)
         w.s.w = p; p += n;
         w.xout = p; p += n;
         w.g.G = p; p += mixed_r1_doubles(m, n);
-        w.g.L = p; p += mixed_r2_doubles(m, n);
+        w.g.L = p; p += mixed_r2_doubles(m, n, P.reg == 2);
         w.g.f = p; p += n;
         w.g.y = p; p += n;
-        w.g.rinv = p; p += n;
+        w.g.dd = p; p += n;
+        w.g.dinv = p; p += n;
         w.g.xp = p; p += n;
         p += 8;
         int *ip = reinterpret_cast<int *>(p);
@@ -135,9 +141,8 @@ __global__ void __launch_bounds__(32) k_voxels(const __grid_constant__ Params P)
         w.g.P = ip + n;
         w.g.pos = ip + 2 * n;
         w.g.lastP = ip + 3 * n;
-        w.g.S = n | 1;
         w.g.lastk = 0;
-        w.As = w.g.L;  // the staged basis is consumed before the first factorization
+        w.As32 = reinterpret_cast<float *>(w.g.L);  // the staged basis is consumed before the first factorization
         w.ldA = m | 1;
         w.s.C = w.g.L;  // GCV singular-value workspace
         w.s.zz = w.g.y;
@@ -242,7 +247,8 @@ struct BasisKey {
 };
 struct Basis {
     double *t2 = nullptr, *logt2 = nullptr, *angles = nullptr, *As = nullptr, *dAs = nullptr, *fixed = nullptr;
-    double *Gs = nullptr;  // Gram matrices of the grid (or fixed) bases, made on first use by the mixed method
+    double *Gs = nullptr;   // packed Gram matrices of the grid (or fixed) bases, made on first use by the mixed method
+    double *AsT = nullptr;  // the same bases transposed (mixed method)
     std::vector<double> h_t2, h_angles;
     size_t bytes = 0;
     long last_use = 0;
@@ -313,7 +319,7 @@ int get_basis(decaes_ctx *ctx, const decaes_t2map_opts &o, Basis **out) {
             if (i->second.last_use < lru->second.last_use) lru = i;
         Basis &b = lru->second;
         cudaFree(b.t2); cudaFree(b.logt2); cudaFree(b.angles); cudaFree(b.As); cudaFree(b.dAs); cudaFree(b.fixed);
-        cudaFree(b.Gs);
+        cudaFree(b.Gs); cudaFree(b.AsT);
         ctx->used -= b.bytes;
         ctx->bases.erase(lru);
     }
@@ -378,12 +384,13 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
     int nl = 0;
     if (mixed && !B->Gs) {
         const int K = fixed ? 1 : o.nRefAngles;
-        const size_t gb = sizeof(double) * (size_t)K * n * n;
-        if (ctx->used + gb > ctx->budget) return fail(ctx, DECAES_ENOMEM, "Gram matrices exceed the HBM budget");
+        const size_t gb = sizeof(double) * (size_t)K * (n * (n + 1) / 2), tb = sizeof(double) * (size_t)K * m * n;
+        if (ctx->used + gb + tb > ctx->budget) return fail(ctx, DECAES_ENOMEM, "Gram matrices exceed the HBM budget");
         CK(cudaMalloc(&B->Gs, gb));
-        B->bytes += gb;
-        ctx->used += gb;
-        dk::k_gram_grid<<<K, 256, 0, st>>>(m, n, fixed ? B->fixed : B->As, B->Gs);
+        CK(cudaMalloc(&B->AsT, tb));
+        B->bytes += gb + tb;
+        ctx->used += gb + tb;
+        dk::k_gram_grid<<<K, 256, 0, st>>>(m, n, fixed ? B->fixed : B->As, B->Gs, B->AsT);
         ++nl;
         CK(cudaGetLastError());
     }
@@ -441,9 +448,11 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
     if (mixed) {
         P.mixed = 1;
         P.Gs = B->Gs;
-        P.epg_lanes_f32 = (int)std::min<long>(32, 2 * dk::mixed_r1_doubles(m, n) / (3L * m));
+        P.AsT = B->AsT;
+        const long rr = dk::mixed_r1_doubles(m, n) + dk::mixed_r2_doubles(m, n, o.Reg == DECAES_REG_GCV);
+        P.epg_lanes_f32 = (int)std::max<long>(1, std::min<long>(32, 2 * rr / (3L * m)));
     }
-    long wsm = mixed ? dk::warp_smem_doubles_mixed(m, n) : dk::warp_smem_doubles(m, n, P.lda);
+    long wsm = mixed ? dk::warp_smem_doubles_mixed(m, n, o.Reg == DECAES_REG_GCV) : dk::warp_smem_doubles(m, n, P.lda);
     size_t smem = (size_t)wsm * sizeof(double);
     if (smem > ctx->smem_optin)
         return fail(ctx, DECAES_EINVAL, "nTE/nT2 too large: the per-voxel workspace (" + std::to_string(smem) +
@@ -583,7 +592,7 @@ extern "C" void decaes_destroy(decaes_ctx *ctx) {
     for (auto &kv : ctx->bases) {
         Basis &b = kv.second;
         cudaFree(b.t2); cudaFree(b.logt2); cudaFree(b.angles); cudaFree(b.As); cudaFree(b.dAs); cudaFree(b.fixed);
-        cudaFree(b.Gs);
+        cudaFree(b.Gs); cudaFree(b.AsT);
     }
     for (auto &e : ctx->ev) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);

@@ -8,8 +8,9 @@
 //   * the passive set grows and shrinks exactly as in Lawson-Hanson (add the
 //     column with the largest positive dual w = f - H x, step back to
 //     feasibility when the unconstrained solution on P leaves the orthant);
-//   * H_PP is held as a Cholesky factor L, extended by one bordered row per
-//     added column and refactored after a removal;
+//   * H_PP is held as an LDL' factorization (unit lower L, pivots D),
+//     extended by one bordered row per added column and refactored
+//     (right-looking) after a removal or a change of mu;
 //   * every solve may start from the previous solve's passive set (the
 //     problem is strictly convex for mu > 0, so any start reaches the same
 //     minimizer): successive mu's of the regularizer searches share most of
@@ -19,28 +20,40 @@
 // per added column O(k) warp instructions on k <= n passive columns instead of
 // O((m+n)(n-k)) for a Householder step.
 //
-// Lane layout: passive rows r live on lanes r and r+32 (n <= 64); G and L are
-// in shared memory with an odd row stride so lanes walking a row or a column
-// hit distinct bank pairs.
+// FP64 results take ~64 cycles to come back on this part, so the factorization
+// avoids square roots and divisions on its dependency chain: LDL' instead of
+// Cholesky, reciprocals seeded in FP32 and finished with one cubic Newton
+// step, unit-diagonal substitutions (one shuffle + one FMA per step), and the
+// trailing update of the factorization as independent FMAs.
+//
+// Storage (shared memory, packed to keep more warps resident): G as its upper
+// triangle by columns, G(i,j) = Gp[j(j+1)/2 + i] for i <= j; L strictly lower
+// by rows, L(r,q) = Lp[r(r-1)/2 + q] for q < r.  Passive rows r live on lanes
+// r and r+32 (n <= 64).
 #pragma once
 #include "nnls_warp.cuh"
 
 namespace dk {
 
 constexpr int kGramMaxN = 64;
-constexpr double kGramDepTol = 1e-12;  // reject a column when d^2 <= tol * H_tt
+constexpr double kGramDepTol = 1e-12;  // reject a column when its pivot <= tol * H_tt
+
+__device__ __forceinline__ int tri(int j) { return (j * (j + 1)) >> 1; }
+// packed symmetric G: entry (i, j)
+__device__ __forceinline__ int gidx(int i, int j) { return i <= j ? tri(j) + i : tri(i) + j; }
 
 struct GramWS {
-    double *G;     // n x S symmetric Gram matrix, G[i + S*j]
-    double *L;     // Cholesky factor of H_PP, row-major lower: L[r*S + q], q <= r
+    double *G;     // packed upper triangle of the Gram matrix, n(n+1)/2
+    double *L;     // packed strictly-lower unit factor of H_PP = L D L'
     double *f;     // A'b
     double *y;     // L^{-1} f_P
-    double *rinv;  // 1 / L[r][r]
+    double *dd;    // pivots D (during a factorization: the running diagonal)
+    double *dinv;  // 1 / D
     double *xp;    // x on P (xp[r] = x[P[r]])
     int *P;        // passive columns, 0-based, k entries
     int *pos;      // pos[j] = index of column j in P, or -1
     int *lastP;    // passive set left by the previous solve (warm start)
-    int S, lastk;
+    int lastk;
     double bb;     // b'b
 };
 
@@ -62,96 +75,153 @@ __device__ __forceinline__ void warp_keymin(long long &key, int &j) {
     }
 }
 
+// 1/d for 1e-30 < d < 1e30: FP32 reciprocal (24 bits) refined by one cubic
+// Newton step r(1 + e + e^2), e = 1 - d r (error ~ e^3, below FP64 rounding).
+__device__ __forceinline__ double fast_rcp(double d) {
+    const double r = (double)__frcp_rn((float)d);
+    const double e = fma(-d, r, 1.0);
+    return fma(r, fma(e, e, e), r);
+}
+
 __device__ __forceinline__ double lane_pick(double v0, double v1, int i) {
     // value held for row i (rows i < 32 in v0, rows >= 32 in v1) broadcast from its lane
     return __shfl_sync(FULL, i < 32 ? v0 : v1, i & 31);
 }
 
-// f = A'b (lanes over columns) and b'b; A column-major with leading
-// dimension lda (odd, in shared memory, so the lanes' columns fall in
-// distinct bank pairs).
-__device__ void gram_rhs(GramWS &g, const double *A, int lda, int m, int n, const double *b) {
+// b'b.
+__device__ void gram_bb(GramWS &g, int m, const double *b) {
     const int lane = threadIdx.x & 31;
-    for (int j = lane; j < n; j += 32) {
-        const double *aj = A + (long)j * lda;
-        double s = 0.0;
-        for (int i = 0; i < m; ++i) s = fma(aj[i], b[i], s);
-        g.f[j] = s;
-    }
     double part = 0.0;
+    #pragma unroll 1
     for (int i = lane; i < m; i += 32) part = fma(b[i], b[i], part);
     g.bb = wsum(part);
+}
+
+// f = A'b from a row-major (transposed, m x n) basis in global memory: lanes
+// over columns, coalesced over each row.
+__device__ __noinline__ void gram_rhs_t(GramWS &g, const double *AT, int m, int n, const double *b) {
+    const int lane = threadIdx.x & 31;
+    #pragma unroll 1
+    for (int j = lane; j < n; j += 32) {
+        double s0 = 0.0, s1 = 0.0;
+        int i = 0;
+        #pragma unroll 1
+        for (; i + 1 < m; i += 2) {
+            s0 = fma(__ldg(AT + (long)i * n + j), b[i], s0);
+            s1 = fma(__ldg(AT + (long)(i + 1) * n + j), b[i + 1], s1);
+        }
+        if (i < m) s0 = fma(__ldg(AT + (long)i * n + j), b[i], s0);
+        g.f[j] = s0 + s1;
+    }
+    gram_bb(g, m, b);
     __syncwarp();
 }
 
-// G = A'A from a basis staged in shared memory (As, column-major with odd
-// leading dimension lda): lanes over the n(n+1)/2 upper-triangle entries.
-__device__ void gram_build(GramWS &g, const double *As, int lda, int m, int n) {
-    const int lane = threadIdx.x & 31, S = g.S;
-    const int npairs = n * (n + 1) / 2;
+// f = A'b and G = A'A from a basis staged in shared memory as FP32 values
+// (column-major, odd leading dimension lda).  The staged values are the FP32
+// EPG curves themselves, so the products are exact in FP64 and G is the Gram
+// matrix of the basis to FP64 rounding.  Lanes over columns for f and over the
+// n(n+1)/2 upper-triangle entries for G.
+__device__ __noinline__ void gram_build_f32(GramWS &g, const float *As, int lda, int m, int n, const double *b) {
+    const int lane = threadIdx.x & 31;
+    #pragma unroll 1
+    for (int j = lane; j < n; j += 32) {
+        const float *aj = As + j * lda;
+        double s0 = 0.0, s1 = 0.0;
+        int i = 0;
+        #pragma unroll 1
+        for (; i + 1 < m; i += 2) {
+            s0 = fma((double)aj[i], b[i], s0);
+            s1 = fma((double)aj[i + 1], b[i + 1], s1);
+        }
+        if (i < m) s0 = fma((double)aj[i], b[i], s0);
+        g.f[j] = s0 + s1;
+    }
+    gram_bb(g, m, b);
+    const int npairs = tri(n);
+    #pragma unroll 1
     for (int p = lane; p < npairs; p += 32) {
-        // p -> (i, j), i <= j, column-by-column enumeration of the upper triangle
         int j = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
-        while (j * (j + 1) / 2 > p) --j;
-        while ((j + 1) * (j + 2) / 2 <= p) ++j;
-        int i = p - j * (j + 1) / 2;
-        const double *ai = As + (long)i * lda, *aj = As + (long)j * lda;
-        double s = 0.0;
-        for (int r = 0; r < m; ++r) s = fma(ai[r], aj[r], s);
-        g.G[i + S * j] = s;
-        g.G[j + S * i] = s;
+        while (tri(j) > p) --j;
+        while (tri(j + 1) <= p) ++j;
+        const int i = p - tri(j);
+        const float *ai = As + i * lda, *aj = As + j * lda;
+        double s0 = 0.0, s1 = 0.0;
+        int r = 0;
+        #pragma unroll 1
+        for (; r + 1 < m; r += 2) {
+            s0 = fma((double)ai[r], (double)aj[r], s0);
+            s1 = fma((double)ai[r + 1], (double)aj[r + 1], s1);
+        }
+        if (r < m) s0 = fma((double)ai[r], (double)aj[r], s0);
+        g.G[p] = s0 + s1;
     }
     __syncwarp();
 }
 
-// G copied from a precomputed n x n matrix in global memory (column-major).
-__device__ void gram_load(GramWS &g, const double *Gg, int n) {
-    const int lane = threadIdx.x & 31, S = g.S;
-    for (int q = lane; q < n * n; q += 32) {
-        int i = q % n, j = q / n;
-        g.G[i + S * j] = __ldg(Gg + q);
-    }
+// G copied from a precomputed packed Gram matrix in global memory.
+__device__ __noinline__ void gram_load(GramWS &g, const double *Gg, int n) {
+    const int lane = threadIdx.x & 31;
+    const int np = tri(n);
+#pragma unroll 4
+    for (int q = lane; q < np; q += 32) g.G[q] = __ldg(Gg + q);
     __syncwarp();
 }
 
-// Cholesky factor of H_PP = G_PP + mu2 I from scratch (left-looking, lanes
-// over rows), then y = L^{-1} f_P.  Returns false when a pivot is not
+// LDL' factorization of H_PP = G_PP + mu2 I from scratch (right-looking,
+// lanes over rows), then y = L^{-1} f_P.  Returns false when a pivot is not
 // positive relative to its diagonal (numerically dependent set).
 __device__ bool gram_refactor(GramWS &g, int k, double mu2) {
-    const int lane = threadIdx.x & 31, S = g.S;
+    const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;
     const int p0 = r0 < k ? g.P[r0] : 0, p1 = r1 < k ? g.P[r1] : 0;
+    double *L0 = g.L + tri(r0 - 1), *L1 = g.L + tri(r1 - 1);
+    // strictly lower triangle and diagonal of H_PP, one row per lane
+    if (r0 < k) {
+        #pragma unroll 1
+        for (int c = 0; c < r0; ++c) L0[c] = g.G[gidx(p0, g.P[c])];
+        g.dd[r0] = g.G[tri(p0) + p0] + mu2;
+    }
+    if (r1 < k) {
+        #pragma unroll 1
+        for (int c = 0; c < r1; ++c) L1[c] = g.G[gidx(p1, g.P[c])];
+        g.dd[r1] = g.G[tri(p1) + p1] + mu2;
+    }
+    __syncwarp();
+    #pragma unroll 1
     for (int j = 0; j < k; ++j) {
+        const double d = g.dd[j];
         const int pj = g.P[j];
-        const double *Lj = g.L + (long)j * S;
-        double s0 = 0.0, s1 = 0.0;
-        if (r0 >= j && r0 < k) {
-            s0 = g.G[p0 + S * pj] + (r0 == j ? mu2 : 0.0);
-            const double *Lr = g.L + (long)r0 * S;
-            for (int q = 0; q < j; ++q) s0 = fma(-Lr[q], Lj[q], s0);
+        const double h = g.G[tri(pj) + pj] + mu2;
+        if (!(d > kGramDepTol * h)) return false;
+        const double rd = fast_rcp(d);
+        double c0 = 0.0, c1 = 0.0, l0 = 0.0, l1 = 0.0;
+        if (r0 > j && r0 < k) { c0 = L0[j]; l0 = c0 * rd; L0[j] = l0; }
+        if (r1 > j && r1 < k) { c1 = L1[j]; l1 = c1 * rd; L1[j] = l1; }
+        if (lane == 0) g.dinv[j] = rd;
+        __syncwarp();
+        // trailing update of row r: columns j < c < r, and the diagonal
+        if (r0 > j && r0 < k) {
+            int bc = tri(j);  // start of row c = j + 1
+            #pragma unroll 1
+            for (int c = j + 1; c < r0; ++c) { L0[c] = fma(-c0, g.L[bc + j], L0[c]); bc += c; }
+            g.dd[r0] = fma(-c0, l0, g.dd[r0]);
         }
-        if (r1 >= j && r1 < k) {
-            s1 = g.G[p1 + S * pj] + (r1 == j ? mu2 : 0.0);
-            const double *Lr = g.L + (long)r1 * S;
-            for (int q = 0; q < j; ++q) s1 = fma(-Lr[q], Lj[q], s1);
+        if (r1 > j && r1 < k) {
+            int bc = tri(j);
+            #pragma unroll 1
+            for (int c = j + 1; c < r1; ++c) { L1[c] = fma(-c1, g.L[bc + j], L1[c]); bc += c; }
+            g.dd[r1] = fma(-c1, l1, g.dd[r1]);
         }
-        const double d2 = lane_pick(s0, s1, j);
-        const double hjj = g.G[pj + S * pj] + mu2;
-        if (!(d2 > kGramDepTol * hjj)) return false;
-        const double d = sqrt(d2), rd = 1.0 / d;
-        if (r0 > j && r0 < k) g.L[(long)r0 * S + j] = s0 * rd;
-        if (r1 > j && r1 < k) g.L[(long)r1 * S + j] = s1 * rd;
-        if (lane == 0) { g.L[(long)j * S + j] = d; g.rinv[j] = rd; }
         __syncwarp();
     }
-    // y = L^{-1} f_P, column-oriented forward substitution
+    // y = L^{-1} f_P (unit lower, column-oriented)
     double v0 = r0 < k ? g.f[p0] : 0.0, v1 = r1 < k ? g.f[p1] : 0.0;
+    #pragma unroll 1
     for (int i = 0; i < k; ++i) {
-        const double yi = lane_pick(v0, v1, i) * g.rinv[i];
-        if (r0 == i) v0 = yi;
-        if (r1 == i) v1 = yi;
-        if (r0 > i && r0 < k) v0 = fma(-g.L[(long)r0 * S + i], yi, v0);
-        if (r1 > i && r1 < k) v1 = fma(-g.L[(long)r1 * S + i], yi, v1);
+        const double ui = lane_pick(v0, v1, i);
+        if (r0 > i && r0 < k) v0 = fma(-L0[i], ui, v0);
+        if (r1 > i && r1 < k) v1 = fma(-L1[i], ui, v1);
     }
     if (r0 < k) g.y[r0] = v0;
     if (r1 < k) g.y[r1] = v1;
@@ -159,36 +229,37 @@ __device__ bool gram_refactor(GramWS &g, int k, double mu2) {
     return true;
 }
 
-// Extends the factor by column t (k -> k+1).  Rejects t when its Schur
-// complement is not positive relative to H_tt or when its coefficient in the
+// Extends the factorization by column t (k -> k+1): u = L^{-1} H[P,t],
+// w = D^{-1} u, delta = H_tt - u'w, y_t = f_t - w'y.  Rejects t when delta is
+// not positive relative to H_tt or when its coefficient y_t / delta in the
 // unconstrained solution on P + {t} is not positive (the guards of the
 // reference's Householder step).  Returns true when t was added.
 __device__ bool gram_append(GramWS &g, int k, int t, double mu2) {
-    const int lane = threadIdx.x & 31, S = g.S;
+    const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;
-    double v0 = r0 < k ? g.G[g.P[r0] + S * t] : 0.0, v1 = r1 < k ? g.G[g.P[r1] + S * t] : 0.0;
+    const double *L0 = g.L + tri(r0 - 1), *L1 = g.L + tri(r1 - 1);
+    double v0 = r0 < k ? g.G[gidx(g.P[r0], t)] : 0.0, v1 = r1 < k ? g.G[gidx(g.P[r1], t)] : 0.0;
+    #pragma unroll 1
     for (int i = 0; i < k; ++i) {
-        const double li = lane_pick(v0, v1, i) * g.rinv[i];
-        if (r0 == i) v0 = li;
-        if (r1 == i) v1 = li;
-        if (r0 > i && r0 < k) v0 = fma(-g.L[(long)r0 * S + i], li, v0);
-        if (r1 > i && r1 < k) v1 = fma(-g.L[(long)r1 * S + i], li, v1);
+        const double ui = lane_pick(v0, v1, i);
+        if (r0 > i && r0 < k) v0 = fma(-L0[i], ui, v0);
+        if (r1 > i && r1 < k) v1 = fma(-L1[i], ui, v1);
     }
-    double pl = 0.0, py = 0.0;
-    if (r0 < k) { pl = fma(v0, v0, pl); py = fma(v0, g.y[r0], py); }
-    if (r1 < k) { pl = fma(v1, v1, pl); py = fma(v1, g.y[r1], py); }
+    double w0 = 0.0, w1 = 0.0, pl = 0.0, py = 0.0;
+    if (r0 < k) { w0 = v0 * g.dinv[r0]; pl = fma(v0, w0, pl); py = fma(w0, g.y[r0], py); }
+    if (r1 < k) { w1 = v1 * g.dinv[r1]; pl = fma(v1, w1, pl); py = fma(w1, g.y[r1], py); }
     const double ll = wsum(pl), ly = wsum(py);
-    const double htt = g.G[t + S * t] + mu2;
-    const double d2 = htt - ll;
-    if (!(d2 > kGramDepTol * htt)) return false;
-    const double d = sqrt(d2);
-    const double yt = (g.f[t] - ly) / d;
+    const double htt = g.G[tri(t) + t] + mu2;
+    const double delta = htt - ll;
+    if (!(delta > kGramDepTol * htt)) return false;
+    const double yt = g.f[t] - ly;
     if (!(yt > 0)) return false;
-    if (r0 < k) g.L[(long)k * S + r0] = v0;
-    if (r1 < k) g.L[(long)k * S + r1] = v1;
+    double *Lk = g.L + tri(k - 1);
+    if (r0 < k) Lk[r0] = w0;
+    if (r1 < k) Lk[r1] = w1;
     if (lane == 0) {
-        g.L[(long)k * S + k] = d;
-        g.rinv[k] = 1.0 / d;
+        g.dd[k] = delta;
+        g.dinv[k] = fast_rcp(delta);
         g.y[k] = yt;
         g.P[k] = t;
         g.pos[t] = k;
@@ -197,32 +268,33 @@ __device__ bool gram_append(GramWS &g, int k, int t, double mu2) {
     return true;
 }
 
-// z = L^{-T} y (back substitution, lanes over rows); z returned in (z0, z1).
+// z = L^{-T} D^{-1} y (unit upper back substitution, lanes over rows);
+// z returned in (z0, z1).
 __device__ void gram_back(const GramWS &g, int k, double &z0, double &z1) {
-    const int lane = threadIdx.x & 31, S = g.S;
+    const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;
-    double u0 = r0 < k ? g.y[r0] : 0.0, u1 = r1 < k ? g.y[r1] : 0.0;
+    double u0 = r0 < k ? g.y[r0] * g.dinv[r0] : 0.0, u1 = r1 < k ? g.y[r1] * g.dinv[r1] : 0.0;
+    #pragma unroll 1
     for (int i = k - 1; i >= 0; --i) {
-        const double zi = lane_pick(u0, u1, i) * g.rinv[i];
-        if (r0 == i) u0 = zi;
-        if (r1 == i) u1 = zi;
-        if (r0 < i) u0 = fma(-g.L[(long)i * S + r0], zi, u0);
-        if (r1 < i) u1 = fma(-g.L[(long)i * S + r1], zi, u1);
+        const double zi = lane_pick(u0, u1, i);
+        const double *Li = g.L + tri(i - 1);
+        if (r0 < i) u0 = fma(-Li[r0], zi, u0);
+        if (r1 < i) u1 = fma(-Li[r1], zi, u1);
     }
     z0 = u0;
     z1 = u1;
 }
 
-// NNLS on H = G + mu2 I with right-hand side f (prepared by gram_rhs and
-// gram_build / gram_load).  On return x (dense, n) holds the solution, idx
+// NNLS on H = G + mu2 I with right-hand side f (prepared by gram_rhs_t /
+// gram_build_f32 / gram_load).  On return x (dense, n) holds the solution, idx
 // its passive columns (1-based, nsetp entries) and rnorm^2 = ||A x - b||^2 +
 // mu2 ||x||^2 with the residual formed explicitly from A (column-major m x n,
-// global or shared).  mode = 1 when max_iter was reached (the reference's
-// iteration cap 3n).
+// global).  mode = 1 when max_iter was reached (the reference's cap 3n).
 __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double *wv, int *idx, const double *A, int m, int n,
                                              const double *b, double mu2, int max_iter, int *lastk_io) {
     const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;
+    #pragma unroll 1
     for (int j = lane; j < n; j += 32) { x[j] = 0.0; g.pos[j] = -1; }
     __syncwarp();
     int k = 0, iters = 0, mode = 0;
@@ -231,11 +303,14 @@ __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double *wv, in
     // solution is positive
     const int lastk = *lastk_io;
     if (lastk > 0) {
+        #pragma unroll 1
         for (int r = lane; r < lastk; r += 32) { g.P[r] = g.lastP[r]; g.pos[g.lastP[r]] = r; }
         __syncwarp();
         k = lastk;
+        #pragma unroll 1
         for (int round = 0; round < kGramMaxN && k > 0; ++round) {
             if (!gram_refactor(g, k, mu2)) {
+                #pragma unroll 1
                 for (int r = lane; r < k; r += 32) g.pos[g.P[r]] = -1;
                 __syncwarp();
                 k = 0;
@@ -271,17 +346,27 @@ __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double *wv, in
 
     unsigned long long rejected = 0ull;  // columns refused since the last change of P (warp-uniform)
     bool dual_stale = true;
+    #pragma unroll 1
     for (int outer = 0;; ++outer) {
         if (outer > 4 * max_iter) { mode = 1; break; }
         // dual w_j = f_j - sum_r G[j, P_r] x_{P_r} on the non-passive columns
         if (dual_stale) {
+            #pragma unroll 1
             for (int r = lane; r < k; r += 32) g.xp[r] = x[g.P[r]];
             __syncwarp();
+            #pragma unroll 1
             for (int j = lane; j < n; j += 32) {
-                double s = g.f[j];
-                if (g.pos[j] < 0)
-                    for (int r = 0; r < k; ++r) s = fma(-g.G[j + g.S * g.P[r]], g.xp[r], s);
-                wv[j] = s;
+                double s = g.f[j], s2 = 0.0;
+                if (g.pos[j] < 0) {
+                    int r = 0;
+                    #pragma unroll 1
+                    for (; r + 1 < k; r += 2) {
+                        s = fma(-g.G[gidx(j, g.P[r])], g.xp[r], s);
+                        s2 = fma(-g.G[gidx(j, g.P[r + 1])], g.xp[r + 1], s2);
+                    }
+                    if (r < k) s = fma(-g.G[gidx(j, g.P[r])], g.xp[r], s);
+                }
+                wv[j] = s + s2;
             }
             __syncwarp();
             dual_stale = false;
@@ -290,6 +375,7 @@ __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double *wv, in
         // entering column: largest positive dual among free, unrefused columns
         long long best = -1;
         int bj = 0x7fffffff;
+        #pragma unroll 1
         for (int j = lane; j < n; j += 32) {
             if (g.pos[j] >= 0 || ((rejected >> j) & 1ull)) continue;
             const double wj = wv[j];
@@ -306,6 +392,7 @@ __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double *wv, in
         k += 1;
         rejected = 0ull;
         // inner loop: move toward the unconstrained solution on P
+        #pragma unroll 1
         for (;;) {
             double z0, z1;
             gram_back(g, k, z0, z1);
@@ -320,8 +407,8 @@ __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double *wv, in
             // alpha = min over z_r <= 0 of x_r / (x_r - z_r)
             double a0 = CUDART_INF, a1 = CUDART_INF;
             const double x0 = r0 < k ? x[g.P[r0]] : 0.0, x1 = r1 < k ? x[g.P[r1]] : 0.0;
-            if (r0 < k && !(z0 > 0)) a0 = (x0 - z0 > 0) ? x0 / (x0 - z0) : 0.0;
-            if (r1 < k && !(z1 > 0)) a1 = (x1 - z1 > 0) ? x1 / (x1 - z1) : 0.0;
+            if (r0 < k && !(z0 > 0)) a0 = (x0 - z0 > 0) ? x0 * fast_rcp(x0 - z0) : 0.0;
+            if (r1 < k && !(z1 > 0)) a1 = (x1 - z1 > 0) ? x1 * fast_rcp(x1 - z1) : 0.0;
             long long ka = okey(a0 <= a1 ? a0 : a1);
             int ia = a0 <= a1 ? r0 : r1;
             warp_keymin(ka, ia);
@@ -350,6 +437,7 @@ __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double *wv, in
             k = __popc(m0) + __popc(m1);
             if (!gram_refactor(g, k, mu2)) {
                 // numerically dependent remainder: restart from the empty set
+                #pragma unroll 1
                 for (int r = lane; r < k; r += 32) { g.pos[g.P[r]] = -1; x[g.P[r]] = 0.0; }
                 __syncwarp();
                 k = 0;
@@ -360,17 +448,28 @@ __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double *wv, in
     }
 
     // outputs: passive list, warm-start set, residual
+    #pragma unroll 1
     for (int r = lane; r < k; r += 32) { idx[r] = g.P[r] + 1; g.lastP[r] = g.P[r]; }
     *lastk_io = k;
     __syncwarp();
+    #pragma unroll 1
     for (int r = lane; r < k; r += 32) g.xp[r] = x[g.P[r]];
     __syncwarp();
     double res = 0.0, xx = 0.0;
+    #pragma unroll 1
     for (int i = lane; i < m; i += 32) {
-        double ri = b[i];
-        for (int r = 0; r < k; ++r) ri = fma(-A[i + (long)m * g.P[r]], g.xp[r], ri);
+        double ri = b[i], ri2 = 0.0;
+        int r = 0;
+        #pragma unroll 1
+        for (; r + 1 < k; r += 2) {
+            ri = fma(-A[i + (long)m * g.P[r]], g.xp[r], ri);
+            ri2 = fma(-A[i + (long)m * g.P[r + 1]], g.xp[r + 1], ri2);
+        }
+        if (r < k) ri = fma(-A[i + (long)m * g.P[r]], g.xp[r], ri);
+        ri += ri2;
         res = fma(ri, ri, res);
     }
+    #pragma unroll 1
     for (int r = lane; r < k; r += 32) xx = fma(g.xp[r], g.xp[r], xx);
     res = wsum(res);
     xx = wsum(xx);

@@ -23,23 +23,12 @@ struct Warp {
     unsigned nnls_caps, loop_caps;
     // mixed method: normal-equation workspace and the staged basis (shared)
     GramWS g;
-    double *As;    // basis staged in shared memory, column-major, leading dimension ldA
+    float *As32;   // FP32 basis staged in shared memory, column-major, leading dimension ldA
     int ldA;
     bool mixed;    // the mixed method (Params::mixed)
 };
 
 __device__ __forceinline__ void note(Warp &w, const NnlsResult &r) { w.nnls_caps += (r.mode != 0); }
-
-// Copies an m x n column-major basis from global memory to w.As (leading
-// dimension ldA), coalesced.
-__device__ void stage_basis(Warp &w, const double *A) {
-    const int m = w.P->m, n = w.P->n;
-    for (long q = w.lane; q < (long)m * n; q += 32) {
-        const int i = (int)(q % m), j = (int)(q / m);
-        w.As[i + (long)w.ldA * j] = A[q];
-    }
-    __syncwarp();
-}
 
 // Unregularized (tikh = false) or Tikhonov solve on the voxel's basis w.A:
 // the reference's Householder NNLS for the plain method, the normal-equation
@@ -66,6 +55,7 @@ __device__ __forceinline__ bool isapprox(double x, double y) {
 // First i in [0, len) with isapprox(x, keys[i]), or -1; lanes over entries.
 __device__ int warp_find_approx(const double *keys, int len, double x) {
     const int lane = threadIdx.x & 31;
+    #pragma unroll 1
     for (int c = 0; c < len; c += 32) {
         int i = c + lane;
         bool hit = i < len && isapprox(x, keys[i]);
@@ -77,6 +67,7 @@ __device__ int warp_find_approx(const double *keys, int len, double x) {
 // First i with keys[i] == x exactly (as doubles), or -1.
 __device__ int warp_find_exact(const double *keys, int len, double x) {
     const int lane = threadIdx.x & 31;
+    #pragma unroll 1
     for (int c = 0; c < len; c += 32) {
         int i = c + lane;
         bool hit = i < len && keys[i] == x;
@@ -90,6 +81,7 @@ __device__ void sol_store(Warp &w, double logmu) {
     if (w.nsol >= kSolCap) return;
     const int n = w.P->n;
     double *dst = w.sol_x + (long)w.nsol * n;
+    #pragma unroll 1
     for (int j = w.lane; j < n; j += 32) dst[j] = w.s.x[j];
     if (w.lane == 0) w.sol_key[w.nsol] = logmu;
     __syncwarp();
@@ -118,6 +110,7 @@ __device__ double tikh_res2(Warp &w, const TikhState &t) {
     return jmax(__dsub_rn(__dmul_rn(t.r.rnorm, t.r.rnorm), __dmul_rn(__dmul_rn(t.mu, t.mu), ssq)), 0.0);
 }
 __device__ void save_x(Warp &w) {
+    #pragma unroll 1
     for (int j = w.lane; j < w.P->n; j += 32) w.xout[j] = w.s.x[j];
     __syncwarp();
 }
@@ -126,6 +119,7 @@ __device__ void final_solution(Warp &w, double logmu) {
     int i = warp_find_exact(w.sol_key, w.nsol, logmu);
     if (i >= 0) {
         const double *src = w.sol_x + (long)i * w.P->n;
+        #pragma unroll 1
         for (int j = w.lane; j < w.P->n; j += 32) w.xout[j] = src[j];
         __syncwarp();
         return;
@@ -176,6 +170,7 @@ __device__ void brent_root(F &f, double x0, double x1, double fx0, double fx1, d
     if (fabs(fa) < fabs(fb)) { double t = a; a = b; b = t; t = fa; fa = fb; fb = t; }
     double c = x0, d = x0, fc = fx0;
     bool mflag = true;
+    #pragma unroll 1
     for (int iter = 1; iter <= maxiters; ++iter) {
         if (fabs(b - a) <= 2 * (xatol + xrtol * fabs(b))) { xr = b; fxr = fb; return; }
         double s = 0;
@@ -325,9 +320,11 @@ __device__ void reg_mdp(Warp &w, double delta, double &mu_out, double &chi2_out)
     double res2_min = __dmul_rn(r0.rnorm, r0.rnorm);
     if (delta <= sqrt(res2_min)) { save_x(w); mu_out = 0; chi2_out = 1; return; }
     double part = 0;
+    #pragma unroll 1
     for (int i = w.lane; i < P.m; i += 32) part = __dadd_rn(part, __dmul_rn(w.data[i], w.data[i]));
     double res2_max = wsum(part);
     if (delta >= sqrt(res2_max)) {
+        #pragma unroll 1
         for (int j = w.lane; j < P.n; j += 32) w.xout[j] = 0.0;
         __syncwarp();
         mu_out = CUDART_INF; chi2_out = res2_max / res2_min;
@@ -401,6 +398,7 @@ __device__ int pc_argmax(const LCurve &L) {
     const int lane = threadIdx.x & 31;
     long long bk = 0;
     int bi = -1;
+    #pragma unroll 1
     for (int c = 0; c < L.plen; c += 32) {
         int i = c + lane;
         if (i < L.plen) {
@@ -434,6 +432,7 @@ struct LcState {
 // found lanes-over-entries with integer keys.
 __device__ void lc_update_curvature(LCurve &L, const LcState &s, const double *Ptl, const double *Pbr, double Ctol) {
     const int lane = threadIdx.x & 31;
+    #pragma unroll 1
     for (int q = 0; q < 4; ++q) {
         double x = s.x[q], P0 = s.P[2 * q], P1 = s.P[2 * q + 1];
         double C = -CUDART_INF;
@@ -441,6 +440,7 @@ __device__ void lc_update_curvature(LCurve &L, const LcState &s, const double *P
             const long long kx = okey(x);
             long long km = 0, kp = 0;
             int im = -1, ip = -1;
+            #pragma unroll 1
             for (int c = 0; c < L.plen; c += 32) {
                 int i = c + lane;
                 if (i < L.plen) {
@@ -473,6 +473,7 @@ __device__ int lc_backtrack(const LCurve &L, double xb, double w0) {
     const int lane = threadIdx.x & 31;
     long long carry = __double_as_longlong(w0);  // widths are >= +0: bit order == value order
     int last = -1;
+    #pragma unroll 1
     for (int c = 0; c < L.slen; c += 32) {
         int k = c + lane;
         bool match = false;
@@ -509,7 +510,9 @@ __device__ double lcurve_corner(LCurve &L, double xlow, double xhigh, double xto
     st.x[3] = xhigh;
     st.x[1] = (PHI * st.x[0] + st.x[3]) / (PHI + 1);
     st.x[2] = st.x[0] + (st.x[3] - st.x[1]);
+    #pragma unroll 1
     for (int i = 0; i < 4; ++i) lc_eval(L, st.x[i], st.P[2 * i], st.P[2 * i + 1]);
+    #pragma unroll 1
     for (int i = 0; i < 4; ++i) pc_set(L, st.x[i], st.P[2 * i], st.P[2 * i + 1], -CUDART_INF, true);
     double Ptl[2] = {st.P[0], st.P[1]}, Pbr[2] = {st.P[6], st.P[7]};
     lc_update_curvature(L, st, Ptl, Pbr, Ctol);
@@ -520,7 +523,9 @@ __device__ double lcurve_corner(LCurve &L, double xlow, double xhigh, double xto
         double xb = L.px[pc_argmax(L)];
         int kb = lc_backtrack(L, xb, fabs(st.x[3] - st.x[0]));
         if (kb >= 0) {
+            #pragma unroll 1
             for (int q = 0; q < 4; ++q) st.x[q] = L.sx[4 * kb + q];
+            #pragma unroll 1
             for (int q = 0; q < 8; ++q) st.P[q] = L.sP[8 * kb + q];
         }
         int i2 = pc_find(L, st.x[1]), i3 = pc_find(L, st.x[2]);
@@ -541,7 +546,9 @@ __device__ double lcurve_corner(LCurve &L, double xlow, double xhigh, double xto
         lc_update_curvature(L, st, Ptl, Pbr, Ctol);
         if (L.slen < kCacheCap) {
             if (L.w->lane == 0) {
+                #pragma unroll 1
                 for (int q = 0; q < 4; ++q) L.sx[4 * L.slen + q] = st.x[q];
+                #pragma unroll 1
                 for (int q = 0; q < 8; ++q) L.sP[8 * L.slen + q] = st.P[q];
             }
             __syncwarp();
@@ -589,16 +596,22 @@ __device__ void warp_svdvals(Warp &w, double *gam) {
     const int r = m >= n ? m : n, c = m >= n ? n : m;
     const int ld = r | 1;
     double *U = w.s.C;  // r x c, ld, fits in the lda x n workspace
+    #pragma unroll 1
     for (int j = 0; j < c; ++j)
+        #pragma unroll 1
         for (int i = lane; i < r; i += 32) U[i + (long)j * ld] = (m >= n) ? w.A[i + (long)j * m] : w.A[j + (long)i * m];
     __syncwarp();
     const double EPS = 2.220446049250313e-16;
+    #pragma unroll 1
     for (int sweep = 0; sweep < 60; ++sweep) {
         double off = 0;
+        #pragma unroll 1
         for (int p = 0; p < c - 1; ++p) {
+            #pragma unroll 1
             for (int q = p + 1; q < c; ++q) {
                 double *up = U + (long)p * ld, *uq = U + (long)q * ld;
                 double pa = 0, pb = 0, pg = 0;
+                #pragma unroll 1
                 for (int i = lane; i < r; i += 32) {
                     double x = up[i], y = uq[i];
                     pa = fma(x, x, pa); pb = fma(y, y, pb); pg = fma(x, y, pg);
@@ -610,6 +623,7 @@ __device__ void warp_svdvals(Warp &w, double *gam) {
                 double zeta = (be - al) / (2 * ga);
                 double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1 + zeta * zeta));
                 double cs = 1 / sqrt(1 + t * t), sn = cs * t;
+                #pragma unroll 1
                 for (int i = lane; i < r; i += 32) {
                     double x = up[i], y = uq[i];
                     up[i] = cs * x - sn * y;
@@ -622,17 +636,21 @@ __device__ void warp_svdvals(Warp &w, double *gam) {
     }
     // column norms, then rank-sort descending
     double *tmp = w.s.zz;
+    #pragma unroll 1
     for (int j = 0; j < c; ++j) {
         const double *u = U + (long)j * ld;
         double part = 0;
+        #pragma unroll 1
         for (int i = lane; i < r; i += 32) part = fma(u[i], u[i], part);
         double sv = sqrt(wsum(part));
         if (lane == 0) tmp[j] = sv;
     }
     __syncwarp();
+    #pragma unroll 1
     for (int j = lane; j < c; j += 32) {
         double v = tmp[j];
         int rank = 0;
+        #pragma unroll 1
         for (int k = 0; k < c; ++k) rank += (tmp[k] > v) || (tmp[k] == v && k < j);
         gam[rank] = v;
     }
@@ -650,6 +668,7 @@ struct GcvF {  // log𝒢(logμ), src/lsqnonneg.jl:1150-1154 and gcv!, 1213-1229
         double res2 = tikh_res2(*w, t);
         int k = P.m < P.n ? P.m : P.n;
         double dof = (double)(P.m - P.n > 0 ? P.m - P.n : 0), l2 = mu * mu;
+        #pragma unroll 1
         for (int i = 0; i < k; ++i) { double g2 = gam[i] * gam[i]; dof += l2 / (g2 + l2); }
         double G = res2 / (dof * dof);
         return pm_log(jmax(G, low));
@@ -699,10 +718,9 @@ __device__ void fa_update(Search &S, int I) {
     const double *A = P.As + (long)(I - 1) * m * n, *dA = P.dAs + (long)(I - 1) * m * n;
     NnlsResult r;
     if (w.mixed) {
-        // precomputed Gram matrix of grid basis I; A'b from the basis staged in shared memory
-        gram_load(w.g, P.Gs + (long)(I - 1) * n * n, n);
-        stage_basis(w, A);
-        gram_rhs(w.g, w.As, w.ldA, m, n, w.data);
+        // precomputed Gram matrix of grid basis I; A'b from its transposed copy
+        gram_load(w.g, P.Gs + (long)(I - 1) * (n * (n + 1) / 2), n);
+        gram_rhs_t(w.g, P.AsT + (long)(I - 1) * m * n, m, n, w.data);
         r = gram_nnls(w.g, w.s.x, w.s.w, w.s.idx, A, m, n, w.data, 0.0, 3 * n, &w.g.lastk);
     } else {
         r = warp_lsq(w.s, A, m, n, w.data, false, 0.0);
@@ -710,10 +728,12 @@ __device__ void fa_update(Search &S, int I) {
     note(w, r);
     double ell = __dmul_rn(r.rnorm, r.rnorm);
     double part = 0;
+    #pragma unroll 1
     for (int i0 = 0; i0 < m; i0 += 32) {
         int i = i0 + lane;
         double ax = 0, dax = 0;
         if (i < m) {
+            #pragma unroll 1
             for (int j = 0; j < n; ++j) {
                 double xj = w.s.x[j];
                 if (xj > 0) {
@@ -730,6 +750,7 @@ __device__ void fa_update(Search &S, int I) {
         S.du[I - 1] = 2 * dt;
         // insertsorted!(idx, I, npts += 1), src/utils.jl:42-49
         int len = S.npts + 1, val = I;
+        #pragma unroll 1
         for (int i = 0; i < len - 1; ++i) {
             int a = S.sidx[i];
             if (val < a) { S.sidx[i] = val; val = a; }
@@ -766,6 +787,7 @@ __device__ void fa_evaluate_box(Search &S, int lo, int hi, bool have_x, double x
 // run with an explicit depth-first stack.
 __device__ void fa_initialize(Search &S) {
     const int K = S.w->P->K;
+    #pragma unroll 1
     for (int depth = 1; depth <= S.mineval; ++depth) {
         // stack of boxes, packed (lo | hi << 9 | depth << 18); 1 <= lo, hi <= 256
         unsigned st[48];
@@ -817,6 +839,7 @@ __device__ void fa_suggest(Search &S, double &xo, double &uo) {
     const double *g = S.w->P->angles;
     int I0 = S.sidx[0];
     double pl = g[I0 - 1], ul = S.u[I0 - 1], dl = S.du[I0 - 1], p = pl, u = ul;
+    #pragma unroll 1
     for (int i = 2; i <= S.npts; ++i) {
         int I = S.sidx[i - 1];
         double pc = g[I - 1], uc = S.u[I - 1], dc = S.du[I - 1], xx, uu;
@@ -831,6 +854,7 @@ __device__ void fa_suggest(Search &S, double &xo, double &uo) {
 __device__ void fa_min_bbox(const Search &S, double x, int &plo, int &phi) {
     const double *g = S.w->P->angles;
     int lo = 1, hi = S.w->P->K;
+    #pragma unroll 1
     for (int guard = 0; guard < 64; ++guard) {
         int mid = (lo + hi) / 2;
         if (g[lo - 1] <= x && x <= g[mid - 1]) {
@@ -852,11 +876,13 @@ __device__ double flip_angle_search(Warp &w) {
     S.u = w.scr + (long)P.m * P.n;
     S.du = S.u + P.K;
     S.sidx = reinterpret_cast<int *>(S.du + P.K);
+    #pragma unroll 1
     for (int q = 0; q < 8; ++q) S.seen[q] = 0;
     S.npts = 0; S.numeval = 0; S.mineval = P.mineval; S.maxeval = P.maxeval;
     fa_initialize(S);
     double x, u;
     fa_suggest(S, x, u);
+    #pragma unroll 1
     for (int guard = 0; guard <= kLoopCap; ++guard) {
         int lo, hi;
         fa_min_bbox(S, x, lo, hi);
@@ -876,6 +902,7 @@ __device__ void warp_basis(Warp &w, double alpha, double *out /* m x n, global *
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lanes = P.epg_lanes, lane = w.lane;
     double *S = w.s.C;  // 3*m*lanes doubles, lane-contiguous
+    #pragma unroll 1
     for (int j0 = 0; j0 < n; j0 += lanes) {
         int j = j0 + lane;
         if (lane < lanes && j < n) {
@@ -895,29 +922,37 @@ __device__ void warp_basis(Warp &w, double alpha, double *out /* m x n, global *
 }
 
 // Mixed method: the same curves with the recursion in FP32 (coefficients in
-// FP64, rounded once), states in the Gram region, written to w.As and then
-// copied to w.A (global) for the fitted curve and the explicit residuals.
+// FP64, rounded once), states in the Gram and factor regions, curves written
+// to w.A (global), rounded to FP32 values and staged in w.As32.  The basis of
+// the voxel is then exactly these FP32 values, for the Gram matrix, the
+// residuals and the fitted curve alike.
 __device__ void warp_basis_f32(Warp &w, double alpha) {
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lanes = P.epg_lanes_f32, lane = w.lane;
     float *S = reinterpret_cast<float *>(w.g.G);  // 3*m*lanes floats, lane-contiguous
+    #pragma unroll 1
     for (int j0 = 0; j0 < n; j0 += lanes) {
         int j = j0 + lane;
         if (lane < lanes && j < n) {
             float *Sl = S + lane;
             if (P.beta180) {
                 dx::FlatCoef<float> q = dx::to_f32(dx::flat_coef(alpha, P.TE, P.t2[j], P.T1));
-                dx::epg_flat_inplace(m, q, Sl, lanes, w.As + (long)j * w.ldA, 1);
+                dx::epg_flat_inplace(m, q, Sl, lanes, w.A + (long)j * m, 1);
             } else {
                 dx::VecCoef<float> q = dx::to_f32(dx::vec_coef(alpha, P.TE, P.t2[j], P.T1, P.beta));
-                dx::epg_vec_inplace(m, q, Sl, lanes, w.As + (long)j * w.ldA, 1);
+                dx::epg_vec_inplace(m, q, Sl, lanes, w.A + (long)j * m, 1);
             }
         }
         __syncwarp();
     }
+    __threadfence_block();
+    __syncwarp();
+    #pragma unroll 1
     for (long q = lane; q < (long)m * n; q += 32) {
         const int i = (int)(q % m), j = (int)(q / m);
-        w.A[q] = w.As[i + (long)w.ldA * j];
+        const float v = (float)w.A[q];
+        w.A[q] = (double)v;
+        w.As32[i + w.ldA * j] = v;
     }
     __threadfence_block();
     __syncwarp();
@@ -932,6 +967,7 @@ __device__ void process_voxel(Warp &w, long v) {
     w.nsol = 0;
     // copy + normalize by the maximum echo
     double mx = 0;
+    #pragma unroll 1
     for (int i = lane; i < m; i += 32) {
         double bi = P.image_f32 ? (double)static_cast<const float *>(P.image)[v + P.V * i]
                                 : static_cast<const double *>(P.image)[v + P.V * i];
@@ -945,6 +981,7 @@ __device__ void process_voxel(Warp &w, long v) {
     }
     __syncwarp();
     if (mx > 0)
+        #pragma unroll 1
         for (int i = lane; i < m; i += 32) w.data[i] = w.data[i] / mx;
     __syncwarp();
 
@@ -953,7 +990,6 @@ __device__ void process_voxel(Warp &w, long v) {
     if (P.angle_mode == 1) {
         alpha = P.fixed_angle;
         w.A = const_cast<double *>(P.basis_fixed);
-        if (w.mixed) stage_basis(w, w.A);
     } else {
         w.A = w.scr;
         if (P.angle_mode == 2) {
@@ -968,9 +1004,12 @@ __device__ void process_voxel(Warp &w, long v) {
         // Gram matrix and right-hand side of the voxel's basis, shared by every
         // solve of the regularizer; GCV's singular values first (their
         // workspace overlaps the staged basis, not the Gram matrix)
-        if (P.angle_mode == 1) gram_load(w.g, P.Gs, n);
-        else gram_build(w.g, w.As, w.ldA, m, n);
-        gram_rhs(w.g, w.As, w.ldA, m, n, w.data);
+        if (P.angle_mode == 1) {
+            gram_load(w.g, P.Gs, n);
+            gram_rhs_t(w.g, P.AsT, m, n, w.data);
+        } else {
+            gram_build_f32(w.g, w.As32, w.ldA, m, n, w.data);
+        }
         if (P.reg == 2) warp_svdvals(w, w.scr + (long)P.m * P.n + 3L * P.K + (long)kCacheCap * 19);
     }
 
@@ -994,6 +1033,7 @@ __device__ void process_voxel(Warp &w, long v) {
 
     // save_results!: rescale, fit, residuals and distribution statistics
     double sd = 0, sr2 = 0, sr = 0, dotl = 0;
+    #pragma unroll 1
     for (int j = lane; j < n; j += 32) {
         double dj = w.xout[j] * mx;
         w.s.w[j] = dj;  // rescaled distribution (w is free now)
@@ -1005,6 +1045,7 @@ __device__ void process_voxel(Warp &w, long v) {
         int i = lane + 32 * t;
         if (i < m) {
             double fit = 0;
+            #pragma unroll 1
             for (int j = 0; j < n; ++j) fit = fma(w.A[i + (long)j * m], w.s.w[j], fit);
             double bi = w.data[i] * mx;
             double ri = fit - bi;
@@ -1014,6 +1055,7 @@ __device__ void process_voxel(Warp &w, long v) {
             if (P.decaycurve) P.decaycurve[v + P.V * i] = fit;
         }
     }
+    #pragma unroll 1
     for (int j = lane; j < n; j += 32) {
         double dj = w.s.w[j];
         sd = __dadd_rn(sd, dj);
@@ -1028,13 +1070,16 @@ __device__ void process_voxel(Warp &w, long v) {
     }
     var = wsum(var);
     double lggm = dotl / sd, lgva = 0;
+    #pragma unroll 1
     for (int j = lane; j < n; j += 32) {
         double d = P.logt2[j] - lggm;
         lgva = __dadd_rn(lgva, __dmul_rn(__dmul_rn(d, d), w.s.w[j]));
     }
     lgva = wsum(lgva) / sd;
+    #pragma unroll 1
     for (int j = lane; j < n; j += 32) P.dist[v + P.V * j] = w.s.w[j];
     if (P.basis_out && P.angle_mode != 1)
+        #pragma unroll 1
         for (long q = lane; q < (long)m * n; q += 32) P.basis_out[v + P.V * q] = w.A[q];
     if (lane == 0) {
         P.gdn[v] = sd;
@@ -1051,6 +1096,7 @@ __device__ void process_voxel(Warp &w, long v) {
     if (P.fuse_t2part) {
         double tsd = 0, ssp = 0, smp = 0, dsp = 0, dmp = 0, dw = 0;
         bool anynan = false;
+        #pragma unroll 1
         for (int j = lane; j < n; j += 32) {
             double d = w.s.w[j];
             anynan |= isnan(d);

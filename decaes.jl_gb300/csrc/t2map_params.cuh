@@ -36,8 +36,9 @@ struct Params {
     int epg_lanes;
     // mixed-precision method (normal-equation NNLS, FP32 EPG at the fitted angle)
     int mixed;
-    const double *Gs;   // Gram matrices A_k'A_k of the grid bases (K x n x n), or of the fixed basis
-    int epg_lanes_f32;  // lanes of the FP32 EPG (states in the Gram region)
+    const double *Gs;   // packed Gram matrices A_k'A_k of the grid bases (K x n(n+1)/2), or of the fixed basis
+    const double *AsT;  // the grid (or fixed) bases transposed, K x m x n (row-major per basis)
+    int epg_lanes_f32;  // lanes of the FP32 EPG (states in the Gram and factor regions)
 };
 
 // Shared-memory footprint of one warp worker (doubles), mirrored on the host.
@@ -48,21 +49,23 @@ __host__ __device__ inline long warp_smem_doubles(int m, int n, int lda) {
     return d + (ints * 4 + bytes + 7) / 8;
 }
 // Shared-memory regions of one warp worker of the mixed method (doubles):
-// R1 holds the Gram matrix (and the FP32 EPG states before it is built), R2
-// the Cholesky factor, the staged basis and the GCV singular-value workspace.
-__host__ __device__ inline long mixed_r1_doubles(int m, int n) {
-    long a = (long)n * (n | 1), b = 3L * m;
-    return a > b ? a : b;
+// R1 holds the packed Gram matrix, R2 the packed factor, or the basis staged
+// in FP32, or (GCV) the singular-value workspace; before the Gram matrix is
+// built both hold the FP32 EPG states.
+__host__ __device__ inline long mixed_r1_doubles(int m, int n) { return (long)n * (n + 1) / 2; }
+__host__ __device__ inline long mixed_r2_doubles(int m, int n, bool gcv) {
+    long l = (long)n * (n - 1) / 2, a = ((long)(m | 1) * n + 1) / 2, e = 2L * m;
+    long x = l > a ? l : a;
+    x = x > e ? x : e;
+    if (gcv) {
+        int r = m >= n ? m : n, c = m >= n ? n : m;
+        long u = (long)(r | 1) * c;
+        x = x > u ? x : u;
+    }
+    return x;
 }
-__host__ __device__ inline long mixed_r2_doubles(int m, int n) {
-    long a = (long)n * (n | 1), b = (long)(m | 1) * n;
-    int r = m >= n ? m : n, c = m >= n ? n : m;
-    long u = (long)(r | 1) * c;
-    long x = a > b ? a : b;
-    return x > u ? x : u;
-}
-__host__ __device__ inline long warp_smem_doubles_mixed(int m, int n) {
-    long d = (long)m + 3L * n + mixed_r1_doubles(m, n) + mixed_r2_doubles(m, n) + 4L * n + 8;
+__host__ __device__ inline long warp_smem_doubles_mixed(int m, int n, bool gcv) {
+    long d = (long)m + 3L * n + mixed_r1_doubles(m, n) + mixed_r2_doubles(m, n, gcv) + 5L * n + 8;
     long ints = 4L * n;  // idx, P, pos, lastP
     return d + (ints * 4 + 7) / 8;
 }
