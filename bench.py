@@ -8,9 +8,14 @@ input; T2part windows SPWin 10-25 ms, MPWin 25-200 ms.  Synthetic, seeded:
 three EPG compartments + Rician noise, 35% background voxels excluded by the
 threshold.  A step is one pass of T2map+T2part over the whole volume.
 
-  value  voxels/s with the image resident in HBM (device-pointer C ABI call)
+  value  voxels/s of the headline method (default: the mixed-precision
+         method) with the image resident in HBM (device-pointer C ABI call)
   e2e    the same metric through the host-buffer C ABI call from pinned
          memory (H2D of the image and D2H of all outputs inside the timing)
+  mixed_vs_fp64  the FP64 (plain) method on the same volume: its voxels/s,
+         the speed-up, and |MWF_mixed - MWF_FP64| over every processed voxel
+         (the method's accuracy gate: p99 <= 1e-3)
+  --precision fp64  makes the FP64 method the headline
   --impl reference  times the CPU restatement of the reference path (the
          oracle, all host threads) on a bounded sample of the same workload.
 """
@@ -147,18 +152,6 @@ def cpu_baseline(mo, img_f32, sample, threads):
     return V / whole, dt, sum(fl.values()) / len(pick), len(pick), len(fg)
 
 
-def traffic_per_voxel():
-    """DRAM bytes per processed voxel of the voxel-solve kernel from the
-    committed ncu summary (None when absent)."""
-    p = os.path.join(ROOT, "profiles", "k_voxels_lcurve48.md")
-    if not os.path.exists(p):
-        return None
-    for line in open(p):
-        if line.startswith("dram_bytes_per_voxel:"):
-            return float(line.split(":")[1])
-    return None
-
-
 def run_reference(args):
     """Times the oracle (CPU restatement of the reference path) on host cores."""
     import decaes_gb300 as D
@@ -191,16 +184,98 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def profile_figure(name, key):
+    """A figure (per voxel) from a committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith(key + ":"):
+            return float(line.split(":")[1])
+    return None
+
+
+class DeviceRun:
+    """Device-resident inputs and outputs (torch owns the memory) and the
+    device-pointer C ABI call of one method."""
+
+    def __init__(self, D, _lib, ctx, torch, mo, po, img, V):
+        self.ctx, self.L, self.torch, self._lib = ctx, ctx.L, torch, _lib
+        n = mo.nT2
+        self.stream = torch.cuda.current_stream()
+        self.d_img = torch.from_numpy(img.reshape(-1, order="F").copy()).cuda()
+        keys = ["dist", "gdn", "ggm", "gva", "fnr", "snr", "alpha"]
+        self.d_out = {"dist": torch.empty(V * n, dtype=torch.float32, device="cuda")}
+        for k in keys[1:]:
+            self.d_out[k] = torch.empty(V, dtype=torch.float32, device="cuda")
+        self.d_parts = {k: torch.empty(V, dtype=torch.float32, device="cuda") for k in ("sfr", "sgm", "mfr", "mgm")}
+        self.mout = _lib.T2mapOutC(*[C.c_void_p(self.d_out[k].data_ptr()) if k in self.d_out else None
+                                     for k, _ in _lib.T2mapOutC._fields_])
+        self.pout = _lib.T2partOutC(*[C.c_void_p(self.d_parts[k].data_ptr()) for k, _ in _lib.T2partOutC._fields_])
+        self.mo_c, self.po_c = mo.to_c(), po.to_c()
+
+    def step(self):
+        self.ctx.check(self.L.decaes_t2map_t2part_device(
+            self.ctx.h, C.byref(self.mo_c), C.byref(self.po_c), C.c_void_p(self.d_img.data_ptr()), self._lib.F32, None,
+            C.byref(self.mout), C.byref(self.pout), C.c_void_p(self.stream.cuda_stream)))
+
+    def stats(self):
+        self.ctx.check(self.L.decaes_sync_stats(self.ctx.h, C.c_void_p(self.stream.cuda_stream)))
+        return self.ctx.stats()
+
+    def timed(self, steps, warmup, world, clocks=None):
+        """W untimed steps, then K steps between barrier + synchronize; returns
+        (ms per step as the max over ranks, kernel launches, voxel-solve ms per step)."""
+        torch = self.torch
+        for _ in range(warmup):
+            self.step()
+        torch.cuda.synchronize()
+        self.stats()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        solve_ms, launches = [], 0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with (clocks if clocks is not None else _Null()):
+            e0.record(self.stream)
+            for _ in range(steps):
+                self.step()
+                st = self.stats()
+                solve_ms.append(st["ms_solve"])
+                launches += st["kernel_launches"]
+            e1.record(self.stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+            dist.barrier()
+        return ms / steps, launches, solve_ms
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
+                    help="method of the headline value; with mixed the FP64 method is measured beside it")
+    ap.add_argument("--no-fp64-compare", action="store_true",
+                    help="skip the FP64 comparison run of the mixed headline")
     ap.add_argument("--matrix", type=int, nargs=3, default=[240, 240, 48])
     ap.add_argument("--seed", type=int, default=2024)
-    ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--cpu-sample", type=int, default=131072)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -223,71 +298,51 @@ def main():
     mo, po, mock = workload(matrix, args.precision)
     img = D.mock_image(mock, seed=args.seed + rank, dtype=np.float32)
     ctx = D.Context(local)
-    L = ctx.L
 
-    # ---- device-resident inputs and outputs (torch owns the memory) ----
-    stream = torch.cuda.current_stream()
-    d_img = torch.from_numpy(img.reshape(-1, order="F").copy()).cuda()
-    n, m = mo.nT2, mo.nTE
-    keys = ["dist", "gdn", "ggm", "gva", "fnr", "snr", "alpha"]
-    d_out = {"dist": torch.empty(V * n, dtype=torch.float32, device="cuda")}
-    for k in keys[1:]:
-        d_out[k] = torch.empty(V, dtype=torch.float32, device="cuda")
-    d_parts = {k: torch.empty(V, dtype=torch.float32, device="cuda") for k in ("sfr", "sgm", "mfr", "mgm")}
-    mout = _lib.T2mapOutC(*[C.c_void_p(d_out[k].data_ptr()) if k in d_out else None for k, _ in _lib.T2mapOutC._fields_])
-    pout = _lib.T2partOutC(*[C.c_void_p(d_parts[k].data_ptr()) for k, _ in _lib.T2partOutC._fields_])
-    mo_c, po_c = mo.to_c(), po.to_c()
-
-    def device_step():
-        ctx.check(L.decaes_t2map_t2part_device(ctx.h, C.byref(mo_c), C.byref(po_c), C.c_void_p(d_img.data_ptr()),
-                                               _lib.F32, None, C.byref(mout), C.byref(pout),
-                                               C.c_void_p(stream.cuda_stream)))
-
-    for _ in range(args.warmup):
-        device_step()
-    torch.cuda.synchronize()
-    ctx.check(L.decaes_sync_stats(ctx.h, C.c_void_p(stream.cuda_stream)))
-    Vp = ctx.stats()["voxels_processed"]
-
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    solve_ms, launches = [], 0
-    with Clocks(local) as clk:
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            device_step()
-            ctx.check(L.decaes_sync_stats(ctx.h, C.c_void_p(stream.cuda_stream)))
-            st = ctx.stats()
-            solve_ms.append(st["ms_solve"])
-            launches += st["kernel_launches"]
-        e1.record(stream)
-        torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
-    ms_per_step = ms / args.steps
-    value = world * V * args.steps / (ms * 1e-3)
+    # ---- headline method, device-resident ----
+    run = DeviceRun(D, _lib, ctx, torch, mo, po, img, V)
+    clk = Clocks(local)
+    ms_per_step, launches, solve_ms = run.timed(args.steps, args.warmup, world, clk)
+    Vp = run.stats()["voxels_processed"]
+    value = world * V / (ms_per_step * 1e-3)
+    sfr_head = run.d_parts["sfr"].double().cpu().numpy()
 
     # ---- end to end through the host-buffer C ABI from pinned memory ----
+    mo_c, po_c = run.mo_c, run.po_c
     h_img = torch.from_numpy(img.reshape(-1, order="F").copy()).pin_memory()
-    h_out = {k: torch.empty_like(v, device="cpu").pin_memory() for k, v in d_out.items()}
-    h_parts = {k: torch.empty_like(v, device="cpu").pin_memory() for k, v in d_parts.items()}
+    h_out = {k: torch.empty_like(v, device="cpu").pin_memory() for k, v in run.d_out.items()}
+    h_parts = {k: torch.empty_like(v, device="cpu").pin_memory() for k, v in run.d_parts.items()}
     hm = _lib.T2mapOutC(*[C.c_void_p(h_out[k].data_ptr()) if k in h_out else None for k, _ in _lib.T2mapOutC._fields_])
     hp = _lib.T2partOutC(*[C.c_void_p(h_parts[k].data_ptr()) for k, _ in _lib.T2partOutC._fields_])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        ctx.check(L.decaes_t2map_t2part(ctx.h, C.byref(mo_c), C.byref(po_c), C.c_void_p(h_img.data_ptr()), _lib.F32,
-                                        None, C.byref(hm), C.byref(hp)))
+        ctx.check(ctx.L.decaes_t2map_t2part(ctx.h, C.byref(mo_c), C.byref(po_c), C.c_void_p(h_img.data_ptr()),
+                                            _lib.F32, None, C.byref(hm), C.byref(hp)))
     e2e_s = (time.perf_counter() - t0) / args.steps
     h2d = img.nbytes
     d2h = sum(v.numel() * 4 for v in h_out.values()) + sum(v.numel() * 4 for v in h_parts.values())
+
+    # ---- the FP64 method on the same volume: throughput and the MWF gate ----
+    compare = None
+    if args.precision == "mixed" and not args.no_fp64_compare:
+        mo64, po64, _ = workload(matrix, "fp64")
+        run64 = DeviceRun(D, _lib, ctx, torch, mo64, po64, img, V)
+        ms64, _, _ = run64.timed(1, 1, world)
+        sfr64 = run64.d_parts["sfr"].double().cpu().numpy()
+        ok = ~np.isnan(sfr64)
+        same_mask = bool(np.array_equal(ok, ~np.isnan(sfr_head)))
+        d = np.abs(sfr_head[ok] - sfr64[ok])
+        compare = {
+            "fp64_value": world * V / (ms64 * 1e-3), "fp64_ms_per_step": ms64,
+            "speedup_vs_fp64": ms64 / ms_per_step,
+            "mwf_abs_err_vs_fp64": {"max": float(d.max()), "p99": float(np.quantile(d, 0.99)),
+                                    "frac_gt_1e-3": float(np.mean(d > 1e-3)), "voxels": int(ok.sum()),
+                                    "same_processed_voxels": same_mask},
+            "gate": "MWF |mixed - FP64| p99 <= 1e-3 over every processed voxel of the volume",
+            "gate_met": bool(np.quantile(d, 0.99) <= 1e-3 and same_mask),
+        }
+        del run64
 
     if rank != 0:
         return
@@ -302,23 +357,40 @@ def main():
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    if compare is not None:
+        line["mixed_vs_fp64"] = compare
     # ---- roofline of the voxel-solve kernel and the CPU baseline ----
     peak = fp64_peak_tflops(torch)
+    kern_ms = statistics.median(solve_ms)
+    cv = None
     if not args.no_cpu_baseline:
         cv, cdt, flops_per_voxel, ns, nfg = cpu_baseline(mo, img, args.cpu_sample, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": cv, "unit": "voxels/s", "cores": os.cpu_count() or 1, "kind": "port",
-                                "sample": f"{ns} above-threshold voxels of the same image ({cdt:.1f} s); "
-                                          f"time scaled to the whole volume"}
-        kern_ms = statistics.median(solve_ms)
-        achieved = flops_per_voxel * Vp / (kern_ms * 1e-3) / 1e12
-        tpv = traffic_per_voxel()
-        line["roofline"] = {"kernel": "k_voxels", "bound": "fp64", "achieved": achieved, "peak": peak,
-                            "unit": "TFLOP/s", "frac": achieved / peak,
-                            "traffic": None if tpv is None else tpv * Vp,
-                            "work": f"{flops_per_voxel / 1e6:.3f} MFLOP FP64 per above-threshold voxel "
-                                    f"(oracle-counted) x {Vp} voxels",
-                            "kernel_ms": kern_ms,
-                            "peak_source": "cuBLAS DGEMM (torch.matmul float64 4096^3) measured in this run"}
+                                "sample": f"{ns} above-threshold voxels of the same image ({cdt:.1f} s, FP64 "
+                                          f"restatement of the reference path); time scaled to the whole volume"}
+    if args.precision == "fp64":
+        if cv is not None:
+            achieved = flops_per_voxel * Vp / (kern_ms * 1e-3) / 1e12
+            tpv = profile_figure("k_voxels_fp64_lcurve48.md", "dram_bytes_per_voxel")  # ncu on a 96x96x1 slab
+            line["roofline"] = {"kernel": "k_voxels (FP64 method)", "bound": "fp64", "achieved": achieved,
+                                "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                                "traffic": None if tpv is None else tpv * Vp,
+                                "work": f"{flops_per_voxel / 1e6:.3f} MFLOP FP64 per above-threshold voxel "
+                                        f"(the reference algorithm, counted by the oracle) x {Vp} voxels",
+                                "kernel_ms": kern_ms,
+                                "peak_source": "cuBLAS DGEMM (torch.matmul float64 4096^3) measured in this run"}
+    else:
+        fpv = profile_figure("k_voxels_mixed_lcurve48.md", "fp64_flops_per_voxel")
+        tpv = profile_figure("k_voxels_mixed_lcurve48.md", "dram_bytes_per_voxel")
+        if fpv is not None:
+            achieved = fpv * Vp / (kern_ms * 1e-3) / 1e12
+            line["roofline"] = {"kernel": "k_voxels (mixed method)", "bound": "fp64", "achieved": achieved,
+                                "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                                "traffic": None if tpv is None else tpv * Vp,
+                                "work": f"{fpv / 1e6:.3f} MFLOP FP64 per above-threshold voxel (executed by the "
+                                        f"mixed method, ncu thread-instruction counts, FMA = 2) x {Vp} voxels",
+                                "kernel_ms": kern_ms,
+                                "peak_source": "cuBLAS DGEMM (torch.matmul float64 4096^3) measured in this run"}
     print(json.dumps(line), flush=True)
 
 
