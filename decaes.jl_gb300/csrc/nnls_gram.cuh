@@ -285,6 +285,151 @@ __device__ void gram_back(const GramWS &g, int k, double &z0, double &z1) {
     z1 = u1;
 }
 
+// Singular values of the basis for GCV, as square roots of the eigenvalues of
+// its Gram matrix (the mixed method's stand-in for svdvals(A)):
+//   1. Householder tridiagonalization of G in a packed lower working copy W
+//      (W(r,c) = W[r(r+1)/2 + c], c <= r: the same packing as G's upper
+//      triangle by columns, so the copy is a straight one), lanes over rows;
+//   2. eigenvalues of the tridiagonal matrix by bisection, one eigenvalue per
+//      lane, counting sign changes of the Sturm sequence p_j = (d_j - x)
+//      p_{j-1} - e_{j-1}^2 p_{j-2} (no divisions on the chain; rescaled by
+//      powers of two when its exponent leaves +-400).
+// Only eigenvalues above tau = 1e-14 * (Gershgorin bound) are resolved: GCV's
+// mu is at least exp(-8), so smaller ones enter its dof sum as 1 either way
+// (error <= tau / mu^2 per eigenvalue).  Eigenvalues are resolved to an
+// absolute 1e-15 * bound.  Writes the min(m,n) largest square roots in
+// descending order to gam (zeros for the unresolved ones).  Uses y, xp, dd and
+// dinv as scratch (free before the first solve) and W (tri(n) doubles).
+__device__ __noinline__ void gram_svdvals(GramWS g, double *W, int m, int n, double *gam) {
+    const int lane = threadIdx.x & 31;
+    const int np = tri(n);
+#pragma unroll 1
+    for (int q = lane; q < np; q += 32) W[q] = g.G[q];
+    __syncwarp();
+    double *d = g.dd, *e = g.dinv, *u = g.y, *qv = g.xp;
+    // 1. tridiagonalization (Householder from the left and right, column k)
+#pragma unroll 1
+    for (int k = 0; k + 2 < n; ++k) {
+        double part = 0.0;
+#pragma unroll 1
+        for (int r = k + 2 + lane; r < n; r += 32) { const double x = W[tri(r) + k]; part = fma(x, x, part); }
+        const double sigma = wsum(part);
+        const double x1 = W[tri(k + 1) + k];
+        if (lane == 0) d[k] = W[tri(k) + k];
+        if (!(sigma > 0)) {  // column already reduced
+            if (lane == 0) e[k] = x1;
+            __syncwarp();
+            continue;
+        }
+        const double nrm = sqrt(fma(x1, x1, sigma));
+        const double alpha = x1 >= 0 ? -nrm : nrm;
+        const double u1 = x1 - alpha;
+        const double beta = 2.0 / fma(u1, u1, sigma);
+        if (lane == 0) e[k] = alpha;
+#pragma unroll 1
+        for (int r = k + 1 + lane; r < n; r += 32) u[r] = (r == k + 1) ? u1 : W[tri(r) + k];
+        __syncwarp();
+        // p = beta W22 u on rows r > k (W symmetric: W(r,c) from row max(r,c))
+        double pk = 0.0;
+#pragma unroll 1
+        for (int r = k + 1 + lane; r < n; r += 32) {
+            const int br = tri(r);
+            double s0 = 0.0, s1 = 0.0;
+            int c = k + 1;
+#pragma unroll 1
+            for (; c + 1 < n; c += 2) {
+                s0 = fma(W[c <= r ? br + c : tri(c) + r], u[c], s0);
+                s1 = fma(W[c + 1 <= r ? br + c + 1 : tri(c + 1) + r], u[c + 1], s1);
+            }
+            if (c < n) s0 = fma(W[c <= r ? br + c : tri(c) + r], u[c], s0);
+            const double pr = beta * (s0 + s1);
+            qv[r] = pr;
+            pk = fma(u[r], pr, pk);
+        }
+        const double K = 0.5 * beta * wsum(pk);
+        __syncwarp();
+#pragma unroll 1
+        for (int r = k + 1 + lane; r < n; r += 32) qv[r] = fma(-K, u[r], qv[r]);
+        __syncwarp();
+        // W22 -= u q' + q u' (lower triangle, row r owned by its lane)
+#pragma unroll 1
+        for (int r = k + 1 + lane; r < n; r += 32) {
+            const int br = tri(r);
+            const double ur = u[r], qr = qv[r];
+#pragma unroll 1
+            for (int c = k + 1; c <= r; ++c) W[br + c] = fma(-ur, qv[c], fma(-qr, u[c], W[br + c]));
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        if (n >= 2) {
+            d[n - 2] = W[tri(n - 2) + n - 2];
+            e[n - 2] = W[tri(n - 1) + n - 2];
+        }
+        d[n - 1] = W[tri(n - 1) + n - 1];
+    }
+    __syncwarp();
+    // squared off-diagonals (reuse W) and the Gershgorin bound
+    double bnd = 0.0;
+#pragma unroll 1
+    for (int j = lane; j < n; j += 32) {
+        const double a = j > 0 ? fabs(e[j - 1]) : 0.0, b = j + 1 < n ? fabs(e[j]) : 0.0;
+        bnd = fmax(bnd, fabs(d[j]) + a + b);
+        if (j + 1 < n) W[j] = e[j] * e[j];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) bnd = fmax(bnd, __shfl_xor_sync(FULL, bnd, o));
+    __syncwarp();
+    const double *e2 = W;
+    const double tau = 1e-14 * bnd, atol = 1e-15 * bnd;
+    // Sturm count: eigenvalues of the tridiagonal matrix below x
+    auto count_below = [&](double x) {
+        double p2 = 1.0, p1 = d[0] - x;
+        bool neg = p1 <= 0;  // a zero takes the sign opposite to its predecessor (p_0 = +1)
+        int c = neg;
+#pragma unroll 1
+        for (int j = 1; j < n; ++j) {
+            double p = fma(d[j] - x, p1, -e2[j - 1] * p2);
+            bool pneg = p < 0 || (p == 0 && !neg);
+            c += (pneg != neg);
+            neg = pneg;
+            p2 = p1;
+            p1 = p;
+            const int ex = ((__double2hiint(p1) >> 20) & 0x7ff) - 1023;
+            if (p1 != 0 && (ex > 400 || ex < -400)) {
+                const double sc = __hiloint2double((1023 - ex) << 20, 0);
+                p1 *= sc;
+                p2 *= sc;
+            }
+        }
+        return c;
+    };
+    const int nz = count_below(tau);  // eigenvalues below tau: left at zero
+    const int kk = m < n ? m : n;
+    const int nres = n - nz;  // resolved eigenvalues (the largest)
+#pragma unroll 1
+    for (int base = 0; base < nres; base += 32) {
+        const int t = base + lane;       // t-th largest eigenvalue
+        const bool mine = t < nres;
+        const int idx = n - 1 - t;       // its index in ascending order
+        double a = tau, b = bnd;
+        bool done = !mine;
+#pragma unroll 1
+        for (int it = 0; it < 80 && __any_sync(FULL, !done); ++it) {
+            const double mid = 0.5 * (a + b);
+            const int c = count_below(mid);
+            if (!done) {
+                if (c > idx) b = mid; else a = mid;
+                done = (b - a) <= fmax(atol, 4.0 * 2.220446049250313e-16 * b);
+            }
+        }
+        if (mine && t < kk) gam[t] = sqrt(0.5 * (a + b));
+    }
+#pragma unroll 1
+    for (int t = nres + lane; t < kk; t += 32) gam[t] = 0.0;
+    __syncwarp();
+}
+
 // NNLS on H = G + mu2 I with right-hand side f (prepared by gram_rhs_t /
 // gram_build_f32 / gram_load).  On return x (dense, n) holds the solution, idx
 // its passive columns (1-based, nsetp entries) and rnorm^2 = ||A x - b||^2 +

@@ -668,8 +668,15 @@ struct GcvF {  // log𝒢(logμ), src/lsqnonneg.jl:1150-1154 and gcv!, 1213-1229
         double res2 = tikh_res2(*w, t);
         int k = P.m < P.n ? P.m : P.n;
         double dof = (double)(P.m - P.n > 0 ? P.m - P.n : 0), l2 = mu * mu;
-        #pragma unroll 1
-        for (int i = 0; i < k; ++i) { double g2 = gam[i] * gam[i]; dof += l2 / (g2 + l2); }
+        if (w->mixed) {  // lanes over singular values
+            double part = 0.0;
+            #pragma unroll 1
+            for (int i = w->lane; i < k; i += 32) { double g2 = gam[i] * gam[i]; part = fma(l2, fast_rcp(g2 + l2), part); }
+            dof += wsum(part);
+        } else {
+            #pragma unroll 1
+            for (int i = 0; i < k; ++i) { double g2 = gam[i] * gam[i]; dof += l2 / (g2 + l2); }
+        }
         double G = res2 / (dof * dof);
         return pm_log(jmax(G, low));
     }
@@ -677,7 +684,7 @@ struct GcvF {  // log𝒢(logμ), src/lsqnonneg.jl:1150-1154 and gcv!, 1213-1229
 __device__ void reg_gcv(Warp &w, double &mu_out, double &chi2_out) {
     const Params &P = *w.P;
     double *gam = w.scr + (long)P.m * P.n + 3L * P.K + (long)kCacheCap * 19;
-    if (!w.mixed) warp_svdvals(w, gam);  // the mixed method computes them before its Gram matrix overwrites the workspace
+    if (!w.mixed) warp_svdvals(w, gam);  // the mixed method takes them from its Gram matrix (gram_svdvals)
     GcvF f{&w, gam, (2.220446049250313e-16 * 2.220446049250313e-16) / P.m};
     double logmu, logG;
     brent_minimize(f, -8.0, 2.0, 0.0, 1e-4, 20, logmu, logG);
@@ -1010,7 +1017,7 @@ __device__ void process_voxel(Warp &w, long v) {
         } else {
             gram_build_f32(w.g, w.As32, w.ldA, m, n, w.data);
         }
-        if (P.reg == 2) warp_svdvals(w, w.scr + (long)P.m * P.n + 3L * P.K + (long)kCacheCap * 19);
+        if (P.reg == 2) gram_svdvals(w.g, w.g.L, m, n, w.scr + (long)P.m * P.n + 3L * P.K + (long)kCacheCap * 19);
     }
 
     double mu = CUDART_NAN, chi2 = CUDART_NAN;

@@ -50,17 +50,16 @@ __host__ __device__ inline long warp_smem_doubles(int m, int n, int lda) {
 }
 // Shared-memory regions of one warp worker of the mixed method (doubles):
 // R1 holds the packed Gram matrix, R2 the packed factor, or the basis staged
-// in FP32, or (GCV) the singular-value workspace; before the Gram matrix is
-// built both hold the FP32 EPG states.
+// in FP32, or (GCV) the tridiagonalization workspace; before the Gram matrix
+// is built both hold the FP32 EPG states.
 __host__ __device__ inline long mixed_r1_doubles(int m, int n) { return (long)n * (n + 1) / 2; }
 __host__ __device__ inline long mixed_r2_doubles(int m, int n, bool gcv) {
     long l = (long)n * (n - 1) / 2, a = ((long)(m | 1) * n + 1) / 2, e = 2L * m;
     long x = l > a ? l : a;
     x = x > e ? x : e;
     if (gcv) {
-        int r = m >= n ? m : n, c = m >= n ? n : m;
-        long u = (long)(r | 1) * c;
-        x = x > u ? x : u;
+        long t = (long)n * (n + 1) / 2;
+        x = x > t ? x : t;
     }
     return x;
 }
