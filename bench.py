@@ -42,24 +42,35 @@ SPWIN, MPWIN = (10e-3, 25e-3), (25e-3, 200e-3)
 THRESHOLD = 200.0
 
 
-def workload(matrix, precision):
+# Workloads: the 48-echo L-curve volume (the headline) and the 56-echo GCV
+# volume of the mixed-precision configuration.
+WORKLOADS = {
+    "lcurve48": dict(matrix=(240, 240, 48), nTE=48, TE=10e-3, nT2=40, T2Range=(10e-3, 2.0), Reg="lcurve", K=32),
+    "gcv56": dict(matrix=(240, 240, 113), nTE=56, TE=7e-3, nT2=60, T2Range=(8e-3, 2.0), Reg="gcv", K=64),
+}
+
+
+def workload(matrix, precision, name="lcurve48"):
     import decaes_gb300 as D
-    mo = D.T2mapOptions(MatrixSize=matrix, nTE=48, TE=10e-3, nT2=40, T2Range=(10e-3, 2.0), Reg="lcurve",
-                        nRefAngles=32, MinRefAngle=50.0, Threshold=THRESHOLD, precision=precision)
+    w = WORKLOADS[name]
+    mo = D.T2mapOptions(MatrixSize=matrix, nTE=w["nTE"], TE=w["TE"], nT2=w["nT2"], T2Range=w["T2Range"], Reg=w["Reg"],
+                        nRefAngles=w["K"], MinRefAngle=50.0, Threshold=THRESHOLD, precision=precision)
     po = D.T2partOptions.from_t2map(mo, SPWin=SPWIN, MPWin=MPWIN)
-    mock = D.MockImageOptions(MatrixSize=matrix, nTE=48, TE=10e-3, BackgroundFraction=0.35)
+    mock = D.MockImageOptions(MatrixSize=matrix, nTE=w["nTE"], TE=w["TE"], BackgroundFraction=0.35)
     return mo, po, mock
 
 
-def config_dict(matrix, precision, V, Vp):
+def config_dict(matrix, precision, V, Vp, name="lcurve48"):
+    w = WORKLOADS[name]
+    img_mb = V * w["nTE"] * 4 / 1e6
     return {
-        "workload": f"{matrix[0]}x{matrix[1]}x{matrix[2]} voxels x 48 echoes, TE=10ms, nT2=40 (10ms-2s), "
-                    f"nRefAngles=32 (spline flip-angle search), Reg=lcurve, Float32 input, "
-                    f"T2part SPWin 10-25ms MPWin 25-200ms",
+        "workload": f"{matrix[0]}x{matrix[1]}x{matrix[2]} voxels x {w['nTE']} echoes, TE={w['TE'] * 1e3:g}ms, "
+                    f"nT2={w['nT2']} ({w['T2Range'][0] * 1e3:g}ms-{w['T2Range'][1]:g}s), nRefAngles={w['K']} "
+                    f"(spline flip-angle search), Reg={w['Reg']}, Float32 input, T2part SPWin 10-25ms MPWin 25-200ms",
         "precision": precision,
         "voxels": V,
         "voxels_above_threshold": Vp,
-        "l2": "inputs larger than L2 (530 MB image vs 129 MB L2); no flush needed",
+        "l2": f"inputs larger than L2 ({img_mb:.0f} MB image vs 129 MB L2); no flush needed",
         "parallelism": "replicas (independent volume per GPU)",
     }
 
@@ -158,8 +169,8 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    matrix = tuple(args.matrix)
-    mo, po, mock = workload(matrix, "fp64")
+    matrix = tuple(args.matrix) if args.matrix else WORKLOADS[args.workload]["matrix"]
+    mo, po, mock = workload(matrix, "fp64", args.workload)
     img = D.mock_image(mock, seed=args.seed, dtype=np.float32)
     threads = os.cpu_count() or 1
     sample = args.cpu_sample
@@ -176,7 +187,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": V / value * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded 3-compartment EPG + Rician noise, 35% background)",
-        "config": config_dict(matrix, "fp64", V, nfg),
+        "config": config_dict(matrix, "fp64", V, nfg, args.workload),
         "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": threads, "kind": "port",
                          "sample": f"{ns} above-threshold voxels per step (of {nfg}); time scaled to the whole volume"},
         "e2e": {"value": value, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -273,11 +284,17 @@ def main():
                     help="method of the headline value; with mixed the FP64 method is measured beside it")
     ap.add_argument("--no-fp64-compare", action="store_true",
                     help="skip the FP64 comparison run of the mixed headline")
-    ap.add_argument("--matrix", type=int, nargs=3, default=[240, 240, 48])
+    ap.add_argument("--workload", default="lcurve48", choices=sorted(WORKLOADS))
+    ap.add_argument("--matrix", type=int, nargs=3, default=None, help="override the workload's MatrixSize")
+    ap.add_argument("--compare-slices", type=int, default=None,
+                    help="z-slices of the volume the FP64 comparison runs on (default: all for lcurve48, 2 for gcv56)")
     ap.add_argument("--seed", type=int, default=2024)
-    ap.add_argument("--cpu-sample", type=int, default=131072)
+    ap.add_argument("--cpu-sample", type=int, default=None,
+                    help="above-threshold voxels the CPU oracle times (default ~10-20 s of 16-core work)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.cpu_sample is None:
+        args.cpu_sample = 131072 if args.workload == "lcurve48" else 16384
     if args.impl == "reference":
         return run_reference(args)
 
@@ -293,9 +310,9 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    matrix = tuple(args.matrix)
+    matrix = tuple(args.matrix) if args.matrix else WORKLOADS[args.workload]["matrix"]
     V = int(np.prod(matrix))
-    mo, po, mock = workload(matrix, args.precision)
+    mo, po, mock = workload(matrix, args.precision, args.workload)
     img = D.mock_image(mock, seed=args.seed + rank, dtype=np.float32)
     ctx = D.Context(local)
 
@@ -326,16 +343,23 @@ def main():
     # ---- the FP64 method on the same volume: throughput and the MWF gate ----
     compare = None
     if args.precision == "mixed" and not args.no_fp64_compare:
-        mo64, po64, _ = workload(matrix, "fp64")
-        run64 = DeviceRun(D, _lib, ctx, torch, mo64, po64, img, V)
+        nz = args.compare_slices or (matrix[2] if args.workload == "lcurve48" else min(2, matrix[2]))
+        nz = max(1, min(nz, matrix[2]))
+        sub = (matrix[0], matrix[1], nz)
+        Vs = int(np.prod(sub))
+        img_s = np.ascontiguousarray(img.reshape((V, -1), order="F")[:Vs]).reshape((*sub, -1), order="F")
+        mo64, po64, _ = workload(sub, "fp64", args.workload)
+        run64 = DeviceRun(D, _lib, ctx, torch, mo64, po64, img_s, Vs)
         ms64, _, _ = run64.timed(1, 1, world)
         sfr64 = run64.d_parts["sfr"].double().cpu().numpy()
+        head_s = sfr_head[:Vs]
         ok = ~np.isnan(sfr64)
-        same_mask = bool(np.array_equal(ok, ~np.isnan(sfr_head)))
-        d = np.abs(sfr_head[ok] - sfr64[ok])
+        same_mask = bool(np.array_equal(ok, ~np.isnan(head_s)))
+        d = np.abs(head_s[ok] - sfr64[ok])
         compare = {
-            "fp64_value": world * V / (ms64 * 1e-3), "fp64_ms_per_step": ms64,
-            "speedup_vs_fp64": ms64 / ms_per_step,
+            "fp64_value": world * Vs / (ms64 * 1e-3), "fp64_ms_per_step": ms64,
+            "fp64_volume": f"{sub[0]}x{sub[1]}x{sub[2]} (first {nz} of {matrix[2]} z-slices)",
+            "speedup_vs_fp64": (world * V / (ms_per_step * 1e-3)) / (world * Vs / (ms64 * 1e-3)),
             "mwf_abs_err_vs_fp64": {"max": float(d.max()), "p99": float(np.quantile(d, 0.99)),
                                     "frac_gt_1e-3": float(np.mean(d > 1e-3)), "voxels": int(ok.sum()),
                                     "same_processed_voxels": same_mask},
@@ -351,7 +375,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
         "data": "synthetic (seeded 3-compartment EPG + Rician noise, 35% background)",
-        "config": config_dict(matrix, args.precision, V, Vp),
+        "config": config_dict(matrix, args.precision, V, Vp, args.workload),
         "e2e": {"value": world * V / e2e_s, "unit": "voxels/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
@@ -371,7 +395,7 @@ def main():
     if args.precision == "fp64":
         if cv is not None:
             achieved = flops_per_voxel * Vp / (kern_ms * 1e-3) / 1e12
-            tpv = profile_figure("k_voxels_fp64_lcurve48.md", "dram_bytes_per_voxel")  # ncu on a 96x96x1 slab
+            tpv = profile_figure(f"k_voxels_fp64_{args.workload}.md", "dram_bytes_per_voxel")  # ncu on a small slab
             line["roofline"] = {"kernel": "k_voxels (FP64 method)", "bound": "fp64", "achieved": achieved,
                                 "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                                 "traffic": None if tpv is None else tpv * Vp,
@@ -380,8 +404,8 @@ def main():
                                 "kernel_ms": kern_ms,
                                 "peak_source": "cuBLAS DGEMM (torch.matmul float64 4096^3) measured in this run"}
     else:
-        fpv = profile_figure("k_voxels_mixed_lcurve48.md", "fp64_flops_per_voxel")
-        tpv = profile_figure("k_voxels_mixed_lcurve48.md", "dram_bytes_per_voxel")
+        fpv = profile_figure(f"k_voxels_mixed_{args.workload}.md", "fp64_flops_per_voxel")
+        tpv = profile_figure(f"k_voxels_mixed_{args.workload}.md", "dram_bytes_per_voxel")
         if fpv is not None:
             achieved = fpv * Vp / (kern_ms * 1e-3) / 1e12
             line["roofline"] = {"kernel": "k_voxels (mixed method)", "bound": "fp64", "achieved": achieved,
