@@ -109,18 +109,12 @@ __global__ void k_compact(const void *image, int f32, long V, double thr, int *v
     }
 }
 
-// Persistent voxel solver: one warp per voxel, voxels pulled from a counter.
-// P.mixed selects the method (warp-uniform for the whole launch).
-__global__ void __launch_bounds__(32) k_voxels(const __grid_constant__ Params P) {
-    extern __shared__ double smem[];
-    Warp w;
+// Points one warp's views at its shared-memory workspace p and global scratch
+// scr for the problem shape of P.
+__device__ void warp_setup(Warp &w, const Params &P, double *p, double *scr) {
     w.P = &P;
-    w.lane = threadIdx.x & 31;
-    w.nnls_caps = 0;
-    w.loop_caps = 0;
     w.mixed = P.mixed != 0;
     const int n = P.n, lda = P.lda;
-    double *p = smem;
     if (w.mixed) {
         // normal-equation workspace (see warp_smem_doubles_mixed)
         const int m = P.m;
@@ -144,7 +138,7 @@ __global__ void __launch_bounds__(32) k_voxels(const __grid_constant__ Params P)
         w.g.lastk = 0;
         w.As32 = reinterpret_cast<float *>(w.g.L);  // the staged basis is consumed before the first factorization
         w.ldA = m | 1;
-        w.s.C = w.g.L;  // GCV singular-value workspace
+        w.s.C = w.g.L;
         w.s.zz = w.g.y;
         w.s.b = nullptr; w.s.rdiag = nullptr; w.s.posof = nullptr; w.s.zl = nullptr; w.s.diag = nullptr;
         w.s.lda = lda;
@@ -164,13 +158,24 @@ __global__ void __launch_bounds__(32) k_voxels(const __grid_constant__ Params P)
         w.s.diag = reinterpret_cast<unsigned char *>(w.s.zl + 2 * n);
         w.s.lda = lda;
     }
-    w.scr = P.scratch + (long)blockIdx.x * P.scr_stride;
-    {
-        const int mn = P.m < P.n ? P.m : P.n;
-        w.sol_key = w.scr + (long)P.m * n + 3L * P.K + (long)kCacheCap * 19 + mn + 16;
-        w.sol_x = w.sol_key + kSolCap;
-        w.nsol = 0;
-    }
+    w.scr = scr;
+    const int mn = P.m < P.n ? P.m : P.n;
+    w.sol_key = w.scr + (long)P.m * n + 3L * P.K + (long)kCacheCap * 19 + mn + 16;
+    w.sol_x = w.sol_key + kSolCap;
+    w.nsol = 0;
+}
+
+// Persistent voxel solver: one warp per voxel, voxels pulled from a counter;
+// blockDim.x / 32 warps per block, each with its own workspace.  P.mixed
+// selects the method (warp-uniform for the whole launch).
+__global__ void __launch_bounds__(128) k_voxels(const __grid_constant__ Params P) {
+    extern __shared__ double smem[];
+    const int wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    Warp w;
+    w.lane = threadIdx.x & 31;
+    w.nnls_caps = 0;
+    w.loop_caps = 0;
+    warp_setup(w, P, smem + (long)wib * P.smem_stride, P.scratch + ((long)blockIdx.x * wpb + wib) * P.scr_stride);
     const int nvox = *P.nvox;
     for (;;) {
         int t = 0;
@@ -182,6 +187,66 @@ __global__ void __launch_bounds__(32) k_voxels(const __grid_constant__ Params P)
     if (w.lane == 0) {
         if (w.nnls_caps) atomicAdd(&P.stats[0], (unsigned long long)w.nnls_caps);
         if (w.loop_caps) atomicAdd(&P.stats[1], (unsigned long long)w.loop_caps);
+    }
+}
+
+// Many volumes in one persistent launch (the batched path).  The compacted
+// voxel lists of all volumes form one queue in the order of B.offsets (the
+// host orders volumes by estimated cost, most expensive first, so the tail of
+// the launch is made of cheap voxels).  A warp that moves to another volume
+// copies that volume's parameters next to its workspace and re-carves the
+// workspace for the volume's (nTE, nT2, method).
+__global__ void __launch_bounds__(128) k_voxels_batch(const __grid_constant__ BatchParams B) {
+    extern __shared__ double smem[];
+    const int wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    double *base = smem + (long)wib * B.smem_stride;
+    Params *Pw = reinterpret_cast<Params *>(base);
+    double *ws = base + kParamsDoubles;
+    double *scr = B.scratch + ((long)blockIdx.x * wpb + wib) * B.scr_stride;
+    Warp w;
+    w.lane = threadIdx.x & 31;
+    w.nnls_caps = 0;
+    w.loop_caps = 0;
+    int cur = -1;
+    const int total = B.offsets[B.nvol];
+    for (;;) {
+        int t = 0;
+        if (w.lane == 0) t = atomicAdd(B.counter, 1);
+        t = __shfl_sync(FULL, t, 0);
+        if (t >= total) break;
+        int lo = 0, hi = B.nvol - 1;  // last volume whose queue segment starts at or before t
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (B.offsets[mid] <= t) lo = mid; else hi = mid - 1;
+        }
+        if (lo != cur) {
+            if (cur >= 0 && w.lane == 0) {
+                if (w.nnls_caps) atomicAdd(&Pw->stats[0], (unsigned long long)w.nnls_caps);
+                if (w.loop_caps) atomicAdd(&Pw->stats[1], (unsigned long long)w.loop_caps);
+            }
+            w.nnls_caps = 0;
+            w.loop_caps = 0;
+            __syncwarp();
+            const double *src = reinterpret_cast<const double *>(B.vols + lo);
+            for (int q = w.lane; q < kParamsDoubles; q += 32) base[q] = src[q];
+            __syncwarp();
+            warp_setup(w, *Pw, ws, scr);
+            cur = lo;
+        }
+        process_voxel(w, (long)Pw->vidx[t - B.offsets[lo]]);
+    }
+    if (cur >= 0 && w.lane == 0) {
+        if (w.nnls_caps) atomicAdd(&Pw->stats[0], (unsigned long long)w.nnls_caps);
+        if (w.loop_caps) atomicAdd(&Pw->stats[1], (unsigned long long)w.loop_caps);
+    }
+}
+
+// offsets[0] = 0, offsets[v + 1] = offsets[v] + counts[v] (one thread; nvol is small).
+__global__ void k_batch_prefix(const int *counts, int nvol, int *offsets) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        int s = 0;
+        offsets[0] = 0;
+        for (int v = 0; v < nvol; ++v) { s += counts[v]; offsets[v + 1] = s; }
     }
 }
 
@@ -252,6 +317,20 @@ struct Basis {
     std::vector<double> h_t2, h_angles;
     size_t bytes = 0;
     long last_use = 0;
+    int pins = 0;  // prepared batches using this basis (not evicted while > 0)
+};
+
+// Autotuning record per problem shape: warps per block of the voxel kernel
+// and the measured cost per voxel.
+struct TuneKey {
+    int m, n, K, reg, mixed, beta180;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(m, n, K, reg, mixed, beta180) < std::tie(o.m, o.n, o.K, o.reg, o.mixed, o.beta180);
+    }
+};
+struct Tune {
+    int wpb = 1;
+    double us_per_voxel = 0;
 };
 
 }  // namespace
@@ -268,6 +347,8 @@ struct decaes_ctx {
     long tick = 0;
     int sms = 0;
     size_t smem_optin = 0;
+    std::map<TuneKey, Tune> tune;
+    int force_wpb = 0;  // autotuner trials
     std::mutex mu;
 };
 
@@ -313,10 +394,11 @@ int get_basis(decaes_ctx *ctx, const decaes_t2map_opts &o, Basis **out) {
         *out = &it->second;
         return DECAES_OK;
     }
-    if (ctx->bases.size() >= 8) {  // evict the least recently used key
-        auto lru = ctx->bases.begin();
+    if (ctx->bases.size() >= 8) {  // evict the least recently used key not held by a prepared batch
+        auto lru = ctx->bases.end();
         for (auto i = ctx->bases.begin(); i != ctx->bases.end(); ++i)
-            if (i->second.last_use < lru->second.last_use) lru = i;
+            if (i->second.pins == 0 && (lru == ctx->bases.end() || i->second.last_use < lru->second.last_use)) lru = i;
+        if (lru == ctx->bases.end()) return fail(ctx, DECAES_ENOMEM, "all resident bases are held by prepared batches");
         Basis &b = lru->second;
         cudaFree(b.t2); cudaFree(b.logt2); cudaFree(b.angles); cudaFree(b.As); cudaFree(b.dAs); cudaFree(b.fixed);
         cudaFree(b.Gs); cudaFree(b.AsT);
@@ -354,6 +436,9 @@ int get_basis(decaes_ctx *ctx, const decaes_t2map_opts &o, Basis **out) {
                                                                   b.angles, b.As, b.dAs, (dx::Dual *)work);
     }
     CK(cudaGetLastError());
+    // callers may enqueue the solve on another stream: the basis is complete
+    // before any of them can read it
+    CK(cudaStreamSynchronize(ctx->stream));
     ctx->used += b.bytes;
     b.last_use = ++ctx->tick;
     auto res = ctx->bases.emplace(key, b);
@@ -368,10 +453,10 @@ struct OutMap {  // device double buffers for each output
 };
 
 // Core: everything on device pointers; host-buffer entry points wrap it with copies.
-int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_opts *po, const void *d_image,
-              int dtype, const void *d_b1, OutMap &out, cudaStream_t st, int *launches) {
+// Shape limits and the resident basis of one volume (plus the mixed method's
+// Gram matrices, made on first use).
+int prepare_basis(decaes_ctx *ctx, const decaes_t2map_opts &o, cudaStream_t st, Basis **out, int *launches) {
     const int m = o.nTE, n = o.nT2;
-    const long V = (long)o.MatrixSize[0] * o.MatrixSize[1] * o.MatrixSize[2];
     if (m > 128) return fail(ctx, DECAES_EINVAL, "nTE > 128 is not supported by this build");
     if (n > 256) return fail(ctx, DECAES_EINVAL, "nT2 > 256 is not supported by this build");
     const bool fixed = !std::isnan(o.SetFlipAngle);
@@ -381,7 +466,6 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
         return fail(ctx, DECAES_EINVAL, "precision = mixed supports nT2 <= " + std::to_string(dk::kGramMaxN));
     Basis *B;
     if (int rc = get_basis(ctx, o, &B)) return rc;
-    int nl = 0;
     if (mixed && !B->Gs) {
         const int K = fixed ? 1 : o.nRefAngles;
         const size_t gb = sizeof(double) * (size_t)K * (n * (n + 1) / 2), tb = sizeof(double) * (size_t)K * m * n;
@@ -390,10 +474,93 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
         CK(cudaMalloc(&B->AsT, tb));
         B->bytes += gb + tb;
         ctx->used += gb + tb;
-        dk::k_gram_grid<<<K, 256, 0, st>>>(m, n, fixed ? B->fixed : B->As, B->Gs, B->AsT);
-        ++nl;
+        dk::k_gram_grid<<<K, 256, 0, ctx->stream>>>(m, n, fixed ? B->fixed : B->As, B->Gs, B->AsT);
+        ++*launches;
         CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(ctx->stream));
     }
+    *out = B;
+    return DECAES_OK;
+}
+
+// Voxel-kernel parameters of one volume, except its queue (nvox, vidx,
+// counter, stats) and scratch fields; *wsm = its shared-memory doubles per warp.
+int make_params(decaes_ctx *ctx, const decaes_t2map_opts &o, const dh::T2partPlan *pp, const double *d_weights,
+                const Basis *B, const void *d_image, int dtype, const void *d_b1, const OutMap &out, dk::Params &P,
+                long *wsm) {
+    const int m = o.nTE, n = o.nT2;
+    const long V = (long)o.MatrixSize[0] * o.MatrixSize[1] * o.MatrixSize[2];
+    const bool fixed = !std::isnan(o.SetFlipAngle), mixed = o.precision == DECAES_PREC_MIXED;
+    P = dk::Params{};
+    P.m = m; P.n = n; P.K = fixed ? 1 : o.nRefAngles; P.M = m + n; P.lda = (m + n) | 1;
+    P.reg = o.Reg; P.chi2factor = o.Chi2Factor; P.noiselevel = o.NoiseLevel;
+    P.mineval = o.nRefAnglesMin; P.maxeval = o.nRefAngles;
+    P.angle_mode = d_b1 ? 2 : (fixed ? 1 : 0);
+    P.fixed_angle = o.SetFlipAngle;
+    P.beta180 = o.RefConAngle == 180.0; P.beta = o.RefConAngle; P.TE = o.TE; P.T1 = o.T1;
+    P.V = V;
+    P.image = d_image; P.image_f32 = dtype == DECAES_F32; P.b1map = d_b1;
+    P.t2 = B->t2; P.logt2 = B->logt2; P.angles = B->angles; P.As = B->As; P.dAs = B->dAs; P.basis_fixed = B->fixed;
+    P.dist = out.dist; P.gdn = out.gdn; P.ggm = out.ggm; P.gva = out.gva; P.fnr = out.fnr; P.snr = out.snr;
+    P.alpha = out.alpha; P.resnorm = out.resnorm; P.decaycurve = out.decaycurve; P.mu = out.mu; P.chi2f = out.chi2f;
+    P.basis_out = out.basis;
+    P.need_chi2 = o.SaveRegParam ? 1 : 0;
+    if (pp) {
+        P.fuse_t2part = 1; P.sp0 = pp->sp0; P.sp1 = pp->sp1; P.mp0 = pp->mp0; P.mp1 = pp->mp1; P.weights = d_weights;
+        P.sfr = out.sfr; P.sgm = out.sgm; P.mfr = out.mfr; P.mgm = out.mgm;
+    }
+    if (mixed) {
+        P.mixed = 1;
+        P.Gs = B->Gs;
+        P.AsT = B->AsT;
+        const long rr = dk::mixed_r1_doubles(m, n) + dk::mixed_r2_doubles(m, n, o.Reg == DECAES_REG_GCV);
+        P.epg_lanes_f32 = (int)std::max<long>(1, std::min<long>(32, 2 * rr / (3L * m)));
+    }
+    P.epg_lanes = (int)std::min<long>(32, ((long)P.lda * n) / (3L * m));
+    P.scr_stride = dk::warp_scratch_doubles(m, n, P.K);
+    *wsm = mixed ? dk::warp_smem_doubles_mixed(m, n, o.Reg == DECAES_REG_GCV) : dk::warp_smem_doubles(m, n, P.lda);
+    *wsm = (*wsm + 1) & ~1L;  // 16-byte aligned warp workspaces
+    if ((size_t)*wsm * sizeof(double) > ctx->smem_optin)
+        return fail(ctx, DECAES_EINVAL, "nTE/nT2 too large: the per-voxel workspace (" +
+                                            std::to_string(*wsm * sizeof(double)) + " bytes) exceeds shared memory per block");
+    return DECAES_OK;
+}
+
+// Warps per block of the voxel kernel for a problem shape (autotuned, else 1).
+int tuned_wpb(decaes_ctx *ctx, const decaes_t2map_opts &o) {
+    if (ctx->force_wpb) return ctx->force_wpb;
+    const bool fixed = !std::isnan(o.SetFlipAngle);
+    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, o.precision == DECAES_PREC_MIXED, o.RefConAngle == 180.0};
+    auto it = ctx->tune.find(k);
+    return it == ctx->tune.end() ? 1 : it->second.wpb;
+}
+
+// Persistent grid for a kernel whose warps each need `stride` doubles of
+// shared memory: blocks of wpb warps, as many as fit on every SM at once.
+template <class Kern>
+int launch_shape(decaes_ctx *ctx, Kern kern, long stride, int *wpb, int *grid, size_t *smem) {
+    for (; *wpb >= 1; *wpb >>= 1) {
+        *smem = (size_t)*wpb * stride * sizeof(double);
+        if (*smem > ctx->smem_optin) continue;
+        CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem));
+        int per_sm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * *wpb, *smem));
+        if (per_sm >= 1) {
+            *grid = per_sm * ctx->sms;
+            return DECAES_OK;
+        }
+    }
+    return fail(ctx, DECAES_EINVAL, "voxel kernel cannot be resident with this workspace size");
+}
+
+// Core: everything on device pointers; host-buffer entry points wrap it with copies.
+int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_opts *po, const void *d_image,
+              int dtype, const void *d_b1, OutMap &out, cudaStream_t st, int *launches) {
+    const long V = (long)o.MatrixSize[0] * o.MatrixSize[1] * o.MatrixSize[2];
+    const int n = o.nT2;
+    int nl = 0;
+    Basis *B;
+    if (int rc = prepare_basis(ctx, o, st, &B, &nl)) return rc;
     // T2part plan (fused)
     dh::T2partPlan pp{};
     double *d_weights = nullptr;
@@ -407,6 +574,9 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
             CK(cudaMemcpyAsync(d_weights, pp.weights.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
         }
     }
+    dk::Params P;
+    long wsm = 0;
+    if (int rc = make_params(ctx, o, po ? &pp : nullptr, d_weights, B, d_image, dtype, d_b1, out, P, &wsm)) return rc;
     // NaN-fill outputs
     {
         int g = std::min<long>(4L * ctx->sms * 8, (long)(out.total + 255) / 256);
@@ -426,50 +596,16 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
         ++nl;
     }
     // persistent voxel kernel
-    dk::Params P{};
-    P.m = m; P.n = n; P.K = fixed ? 1 : o.nRefAngles; P.M = m + n; P.lda = (m + n) | 1;
-    P.reg = o.Reg; P.chi2factor = o.Chi2Factor; P.noiselevel = o.NoiseLevel;
-    P.mineval = o.nRefAnglesMin; P.maxeval = o.nRefAngles;
-    P.angle_mode = d_b1 ? 2 : (fixed ? 1 : 0);
-    P.fixed_angle = o.SetFlipAngle;
-    P.beta180 = o.RefConAngle == 180.0; P.beta = o.RefConAngle; P.TE = o.TE; P.T1 = o.T1;
-    P.V = V; P.nvox = d_nvox; P.vidx = (const int *)vidx;
-    P.image = d_image; P.image_f32 = dtype == DECAES_F32; P.b1map = d_b1;
-    P.t2 = B->t2; P.logt2 = B->logt2; P.angles = B->angles; P.As = B->As; P.dAs = B->dAs; P.basis_fixed = B->fixed;
-    P.counter = d_counter; P.stats = d_stats;
-    P.dist = out.dist; P.gdn = out.gdn; P.ggm = out.ggm; P.gva = out.gva; P.fnr = out.fnr; P.snr = out.snr;
-    P.alpha = out.alpha; P.resnorm = out.resnorm; P.decaycurve = out.decaycurve; P.mu = out.mu; P.chi2f = out.chi2f;
-    P.basis_out = out.basis;
-    P.need_chi2 = o.SaveRegParam ? 1 : 0;
-    if (po) {
-        P.fuse_t2part = 1; P.sp0 = pp.sp0; P.sp1 = pp.sp1; P.mp0 = pp.mp0; P.mp1 = pp.mp1; P.weights = d_weights;
-        P.sfr = out.sfr; P.sgm = out.sgm; P.mfr = out.mfr; P.mgm = out.mgm;
-    }
-    if (mixed) {
-        P.mixed = 1;
-        P.Gs = B->Gs;
-        P.AsT = B->AsT;
-        const long rr = dk::mixed_r1_doubles(m, n) + dk::mixed_r2_doubles(m, n, o.Reg == DECAES_REG_GCV);
-        P.epg_lanes_f32 = (int)std::max<long>(1, std::min<long>(32, 2 * rr / (3L * m)));
-    }
-    long wsm = mixed ? dk::warp_smem_doubles_mixed(m, n, o.Reg == DECAES_REG_GCV) : dk::warp_smem_doubles(m, n, P.lda);
-    size_t smem = (size_t)wsm * sizeof(double);
-    if (smem > ctx->smem_optin)
-        return fail(ctx, DECAES_EINVAL, "nTE/nT2 too large: the per-voxel workspace (" + std::to_string(smem) +
-                                            " bytes) exceeds shared memory per block");
-    P.epg_lanes = (int)std::min<long>(32, ((long)P.lda * n) / (3L * m));
-    auto kern = dk::k_voxels;
-    CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem));
-    if (per_sm < 1) return fail(ctx, DECAES_EINVAL, "voxel kernel cannot be resident with this workspace size");
-    const int grid = per_sm * ctx->sms;
-    P.scr_stride = dk::warp_scratch_doubles(m, n, P.K);
+    P.nvox = d_nvox; P.vidx = (const int *)vidx; P.counter = d_counter; P.stats = d_stats;
+    P.smem_stride = wsm;
+    int wpb = tuned_wpb(ctx, o), grid = 0;
+    size_t smem = 0;
+    if (int rc = launch_shape(ctx, dk::k_voxels, wsm, &wpb, &grid, &smem)) return rc;
     void *scr;
-    if (int rc = buf(ctx, "scratch", sizeof(double) * (size_t)P.scr_stride * grid, &scr)) return rc;
+    if (int rc = buf(ctx, "scratch", sizeof(double) * (size_t)P.scr_stride * grid * wpb, &scr)) return rc;
     P.scratch = (double *)scr;
     cudaEventRecord(ctx->ev[2], st);
-    kern<<<grid, 32, smem, st>>>(P);
+    dk::k_voxels<<<grid, 32 * wpb, smem, st>>>(P);
     cudaEventRecord(ctx->ev[3], st);
     ++nl;
     CK(cudaGetLastError());
@@ -477,7 +613,9 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
     return DECAES_OK;
 }
 
-int out_layout(decaes_ctx *ctx, const decaes_t2map_opts &o, bool want_t2part, OutMap &om) {
+// FP64 output buffers of one volume carved from d (d = nullptr: size only);
+// returns the doubles needed.
+size_t layout_outputs(const decaes_t2map_opts &o, bool want_t2part, double *d, OutMap &om) {
     const long V = (long)o.MatrixSize[0] * o.MatrixSize[1] * o.MatrixSize[2];
     const bool fixed = !std::isnan(o.SetFlipAngle);
     size_t tot = 0;
@@ -488,9 +626,7 @@ int out_layout(decaes_ctx *ctx, const decaes_t2map_opts &o, bool want_t2part, Ou
     size_t o_mu = o.SaveRegParam ? take(V) : SIZE_MAX, o_chi = o.SaveRegParam ? take(V) : SIZE_MAX;
     size_t o_basis = (o.SaveNNLSBasis && !fixed) ? take((size_t)V * o.nTE * o.nT2) : SIZE_MAX;
     size_t o_part = want_t2part ? take((size_t)V * 4) : SIZE_MAX;
-    void *p;
-    if (int rc = buf(ctx, "outputs", sizeof(double) * tot, &p)) return rc;
-    double *d = (double *)p;
+    if (!d) return tot;
     auto at = [&](size_t off) { return off == SIZE_MAX ? nullptr : d + off; };
     om.dist = at(o_dist);
     om.gdn = d + o_maps; om.ggm = om.gdn + V; om.gva = om.ggm + V; om.fnr = om.gva + V; om.snr = om.fnr + V; om.alpha = om.snr + V;
@@ -498,6 +634,15 @@ int out_layout(decaes_ctx *ctx, const decaes_t2map_opts &o, bool want_t2part, Ou
     double *pt = at(o_part);
     om.sfr = pt; om.sgm = pt ? pt + V : nullptr; om.mfr = pt ? pt + 2 * V : nullptr; om.mgm = pt ? pt + 3 * V : nullptr;
     om.total = tot;
+    return tot;
+}
+
+int out_layout(decaes_ctx *ctx, const decaes_t2map_opts &o, bool want_t2part, OutMap &om) {
+    OutMap tmp;
+    const size_t tot = layout_outputs(o, want_t2part, nullptr, tmp);
+    void *p;
+    if (int rc = buf(ctx, "outputs", sizeof(double) * tot, &p)) return rc;
+    layout_outputs(o, want_t2part, (double *)p, om);
     return DECAES_OK;
 }
 
@@ -799,5 +944,368 @@ extern "C" int decaes_t2part(decaes_ctx *ctx, const decaes_t2part_opts *opts, co
     ctx->stats.voxels = V;
     ctx->stats.ms_total = t;
     ctx->stats.kernel_launches = launches;
+    return DECAES_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched volumes: one persistent launch over many volumes
+// ---------------------------------------------------------------------------
+namespace {
+
+struct BatchVol {
+    decaes_volume v;
+    Basis *B = nullptr;
+    dh::T2partPlan pp{};
+    bool t2part = false;
+    long V = 0;
+    double cost = 0;
+    size_t out_off = 0, out_len = 0, vidx_off = 0, w_off = SIZE_MAX;
+    OutMap om{};
+};
+
+// Working memory and launch shape of a batch.  The buffers are the context's
+// named buffers (one-shot call) or allocations the prepared batch owns.
+struct BatchPrep {
+    std::vector<BatchVol> vols;  // queue order: most expensive first
+    size_t n_out = 0, n_vidx = 0, n_w = 0;
+    double *outs = nullptr, *weights = nullptr, *scratch = nullptr;
+    int *vidx = nullptr, *cnt = nullptr;  // cnt: counts[nvol], offsets[nvol + 1], counter
+    unsigned long long *stats = nullptr;  // 2 per volume
+    dk::Params *params = nullptr;
+    long smem_stride = 0, scr_stride = 0;
+    int wpb = 1, grid = 0;
+    size_t smem = 0;
+    size_t cnt_bytes() const { return sizeof(int) * (2 * vols.size() + 2) + 16; }
+};
+
+// Relative cost of a voxel: the autotuner's measurement, else a model of the
+// methods' measured costs (FP64 GCV ~35x the mixed method, FP64 ~5x mixed).
+double voxel_cost(decaes_ctx *ctx, const decaes_t2map_opts &o) {
+    const bool fixed = !std::isnan(o.SetFlipAngle), mixed = o.precision == DECAES_PREC_MIXED;
+    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, mixed, o.RefConAngle == 180.0};
+    auto it = ctx->tune.find(k);
+    if (it != ctx->tune.end() && it->second.us_per_voxel > 0) return it->second.us_per_voxel;
+    double c = 1e-4 * o.nTE * o.nT2;
+    if (o.Reg == DECAES_REG_LCURVE || o.Reg == DECAES_REG_GCV) c *= 3;
+    if (!mixed) c *= (o.Reg == DECAES_REG_GCV) ? 35 : 5;
+    return c;
+}
+
+int batch_plan(decaes_ctx *ctx, const decaes_volume *vols, int nvol, cudaStream_t st, BatchPrep &bp, int *launches) {
+    if (!vols || nvol < 1) return fail(ctx, DECAES_EINVAL, "a batch needs at least one volume");
+    bp.vols.clear();
+    for (int i = 0; i < nvol; ++i) {
+        const decaes_volume &v = vols[i];
+        const decaes_t2part_opts *po = v.has_t2part ? &v.popts : nullptr;
+        if (int rc = check_both(ctx, &v.mopts, po, v.dtype)) return rc;
+        const decaes_t2map_out &o = v.d_mout;
+        if (!v.d_image || !o.dist || !o.gdn || !o.ggm || !o.gva || !o.fnr || !o.snr || !o.alpha)
+            return fail(ctx, DECAES_EINVAL, "batch volume " + std::to_string(i) + ": image, dist and the six maps are required");
+        if (o.echotimes || o.t2times || o.refangleset || o.decaybasisset)
+            return fail(ctx, DECAES_EINVAL, "batch volume " + std::to_string(i) + ": per-call constant outputs must be NULL");
+        if (po && (!v.d_pout.sfr || !v.d_pout.sgm || !v.d_pout.mfr || !v.d_pout.mgm))
+            return fail(ctx, DECAES_EINVAL, "batch volume " + std::to_string(i) + ": T2part outputs are required");
+        BatchVol bv;
+        bv.v = v;
+        bv.t2part = po != nullptr;
+        if (int rc = prepare_basis(ctx, v.mopts, st, &bv.B, launches)) return rc;
+        if (po) {
+            std::string e = dh::t2part_plan(*po, bv.pp);
+            if (!e.empty()) return fail(ctx, DECAES_EINVAL, e);
+        }
+        bv.V = (long)v.mopts.MatrixSize[0] * v.mopts.MatrixSize[1] * v.mopts.MatrixSize[2];
+        bv.cost = voxel_cost(ctx, v.mopts) * (double)bv.V;
+        bp.vols.push_back(bv);
+    }
+    std::stable_sort(bp.vols.begin(), bp.vols.end(), [](const BatchVol &a, const BatchVol &b) { return a.cost > b.cost; });
+    bp.n_out = bp.n_vidx = bp.n_w = 0;
+    bp.smem_stride = bp.scr_stride = 0;
+    for (BatchVol &bv : bp.vols) {
+        OutMap tmp;
+        bv.out_len = layout_outputs(bv.v.mopts, bv.t2part, nullptr, tmp);
+        bv.out_off = bp.n_out;
+        bp.n_out += (bv.out_len + 1) & ~size_t(1);
+        bv.vidx_off = bp.n_vidx;
+        bp.n_vidx += (size_t)std::max<long>(bv.V, 1);
+        bv.w_off = SIZE_MAX;
+        if (bv.t2part && !bv.pp.weights.empty()) { bv.w_off = bp.n_w; bp.n_w += bv.v.mopts.nT2; }
+        dk::Params P;
+        long wsm = 0;
+        if (int rc = make_params(ctx, bv.v.mopts, nullptr, nullptr, bv.B, nullptr, bv.v.dtype, nullptr, tmp, P, &wsm)) return rc;
+        bp.smem_stride = std::max(bp.smem_stride, (long)dk::kParamsDoubles + wsm);
+        bp.scr_stride = std::max(bp.scr_stride, P.scr_stride);
+    }
+    bp.smem_stride = (bp.smem_stride + 1) & ~1L;
+    bp.wpb = tuned_wpb(ctx, bp.vols[0].v.mopts);
+    return launch_shape(ctx, dk::k_voxels_batch, bp.smem_stride, &bp.wpb, &bp.grid, &bp.smem);
+}
+
+size_t batch_bytes(const BatchPrep &bp, size_t *b_out, size_t *b_vidx, size_t *b_w, size_t *b_par, size_t *b_scr) {
+    *b_out = sizeof(double) * std::max<size_t>(bp.n_out, 1);
+    *b_vidx = sizeof(int) * std::max<size_t>(bp.n_vidx, 1);
+    *b_w = sizeof(double) * std::max<size_t>(bp.n_w, 1);
+    *b_par = sizeof(dk::Params) * bp.vols.size() + bp.cnt_bytes() + 16 * bp.vols.size();
+    *b_scr = sizeof(double) * (size_t)bp.scr_stride * bp.grid * bp.wpb;
+    return *b_out + *b_vidx + *b_w + *b_par + *b_scr;
+}
+
+// Points the batch at its buffers and uploads the per-volume parameters and
+// T2part weights (synchronous copies: done once, before any capture).
+int batch_bind(decaes_ctx *ctx, BatchPrep &bp, void *outs, void *vidx, void *w, void *par, void *scr) {
+    const int nvol = (int)bp.vols.size();
+    bp.outs = (double *)outs; bp.vidx = (int *)vidx; bp.weights = (double *)w; bp.scratch = (double *)scr;
+    bp.params = (dk::Params *)par;
+    char *tail = (char *)par + sizeof(dk::Params) * nvol;
+    bp.stats = (unsigned long long *)tail;
+    bp.cnt = (int *)(tail + 16 * nvol);
+    std::vector<dk::Params> hp(nvol);
+    for (int q = 0; q < nvol; ++q) {
+        BatchVol &bv = bp.vols[q];
+        layout_outputs(bv.v.mopts, bv.t2part, bp.outs + bv.out_off, bv.om);
+        const double *wts = nullptr;
+        if (bv.w_off != SIZE_MAX) {
+            wts = bp.weights + bv.w_off;
+            CK(cudaMemcpy((void *)wts, bv.pp.weights.data(), sizeof(double) * bv.v.mopts.nT2, cudaMemcpyHostToDevice));
+        }
+        long wsm = 0;
+        if (int rc = make_params(ctx, bv.v.mopts, bv.t2part ? &bv.pp : nullptr, wts, bv.B, bv.v.d_image, bv.v.dtype,
+                                 bv.v.d_b1map, bv.om, hp[q], &wsm))
+            return rc;
+        hp[q].vidx = bp.vidx + bv.vidx_off;
+        hp[q].nvox = bp.cnt + q;
+        hp[q].stats = bp.stats + 2 * q;
+    }
+    CK(cudaMemcpy(bp.params, hp.data(), sizeof(dk::Params) * nvol, cudaMemcpyHostToDevice));
+    return DECAES_OK;
+}
+
+// The batch's launch sequence on st: memsets, kernels and device copies only,
+// so it can be captured into a CUDA graph.
+int batch_enqueue(decaes_ctx *ctx, const BatchPrep &bp, cudaStream_t st, int *launches) {
+    const int nvol = (int)bp.vols.size();
+    int *counts = bp.cnt, *offsets = bp.cnt + nvol, *counter = bp.cnt + 2 * nvol + 1;
+    CK(cudaMemsetAsync(bp.cnt, 0, bp.cnt_bytes(), st));
+    CK(cudaMemsetAsync(bp.stats, 0, 16 * nvol, st));
+    for (int q = 0; q < nvol; ++q) {
+        const BatchVol &bv = bp.vols[q];
+        int g = (int)std::min<long>(4L * ctx->sms * 8, (long)(bv.out_len + 255) / 256);
+        dk::k_fill<<<std::max(g, 1), 256, 0, st>>>(bp.outs + bv.out_off, (long)bv.out_len, NAN);
+        g = (int)std::min<long>(8L * ctx->sms, (bv.V + 255) / 256);
+        dk::k_compact<<<std::max(g, 1), 256, 0, st>>>(bv.v.d_image, bv.v.dtype == DECAES_F32, bv.V, bv.v.mopts.Threshold,
+                                                      bp.vidx + bv.vidx_off, counts + q);
+        *launches += 2;
+    }
+    dk::k_batch_prefix<<<1, 32, 0, st>>>(counts, nvol, offsets);
+    dk::BatchParams B{bp.params, offsets, nvol, counter, bp.scratch, bp.scr_stride, bp.smem_stride};
+    dk::k_voxels_batch<<<bp.grid, 32 * bp.wpb, bp.smem, st>>>(B);
+    *launches += 2;
+    for (int q = 0; q < nvol; ++q) {
+        const BatchVol &bv = bp.vols[q];
+        const decaes_t2map_out &d = bv.v.d_mout;
+        const OutMap &om = bv.om;
+        const size_t V = (size_t)bv.V, n = bv.v.mopts.nT2, m = bv.v.mopts.nTE;
+        struct { const double *s; void *d; size_t len; } cp[] = {
+            {om.dist, d.dist, V * n}, {om.gdn, d.gdn, V}, {om.ggm, d.ggm, V}, {om.gva, d.gva, V}, {om.fnr, d.fnr, V},
+            {om.snr, d.snr, V}, {om.alpha, d.alpha, V}, {om.resnorm, d.resnorm, V}, {om.decaycurve, d.decaycurve, V * m},
+            {om.mu, d.mu, V}, {om.chi2f, d.chi2factor, V}, {om.basis, d.decaybasis, V * m * n},
+            {om.sfr, bv.t2part ? bv.v.d_pout.sfr : nullptr, V}, {om.sgm, bv.t2part ? bv.v.d_pout.sgm : nullptr, V},
+            {om.mfr, bv.t2part ? bv.v.d_pout.mfr : nullptr, V}, {om.mgm, bv.t2part ? bv.v.d_pout.mgm : nullptr, V},
+        };
+        for (auto &c : cp) {
+            if (!c.s || !c.d) continue;
+            if (bv.v.dtype == DECAES_F64) {
+                CK(cudaMemcpyAsync(c.d, c.s, sizeof(double) * c.len, cudaMemcpyDeviceToDevice, st));
+            } else {
+                int g = (int)std::min<long>(8L * ctx->sms, ((long)c.len + 255) / 256);
+                dk::k_narrow<<<std::max(g, 1), 256, 0, st>>>(c.s, (float *)c.d, (long)c.len);
+                ++*launches;
+            }
+        }
+    }
+    CK(cudaGetLastError());
+    return DECAES_OK;
+}
+
+}  // namespace
+
+struct decaes_batch {
+    decaes_ctx *ctx = nullptr;
+    BatchPrep bp;
+    std::vector<void *> owned;
+    size_t owned_bytes = 0;
+    std::vector<Basis *> pinned;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int launches = 0;
+};
+
+extern "C" int decaes_t2map_t2part_batch(decaes_ctx *ctx, const decaes_volume *vols, int32_t nvol, void *stream) {
+    if (!ctx) return DECAES_EINVAL;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    int launches = 0;
+    ctx->stats = decaes_stats{};
+    BatchPrep bp;
+    if (int rc = batch_plan(ctx, vols, nvol, st, bp, &launches)) return rc;
+    size_t b_out, b_vidx, b_w, b_par, b_scr;
+    batch_bytes(bp, &b_out, &b_vidx, &b_w, &b_par, &b_scr);
+    void *outs, *vidx, *w, *par, *scr;
+    if (int rc = buf(ctx, "batch_outputs", b_out, &outs)) return rc;
+    if (int rc = buf(ctx, "batch_vidx", b_vidx, &vidx)) return rc;
+    if (int rc = buf(ctx, "batch_weights", b_w, &w)) return rc;
+    if (int rc = buf(ctx, "batch_params", b_par, &par)) return rc;
+    if (int rc = buf(ctx, "scratch", b_scr, &scr)) return rc;
+    CK(cudaStreamSynchronize(st));  // the named buffers may still be in use by earlier work on this stream
+    if (int rc = batch_bind(ctx, bp, outs, vidx, w, par, scr)) return rc;
+    if (int rc = batch_enqueue(ctx, bp, st, &launches)) return rc;
+    long V = 0;
+    for (auto &bv : bp.vols) V += bv.V;
+    ctx->stats.voxels = V;
+    ctx->stats.solve_launches = 1;
+    ctx->stats.kernel_launches = launches;
+    return DECAES_OK;
+}
+
+extern "C" decaes_batch *decaes_batch_create(decaes_ctx *ctx, const decaes_volume *vols, int32_t nvol) {
+    if (!ctx) return nullptr;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    auto *b = new decaes_batch();
+    b->ctx = ctx;
+    auto bail = [&](int) {
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        if (b->cap) cudaStreamDestroy(b->cap);
+        for (void *p : b->owned) cudaFree(p);
+        ctx->used -= b->owned_bytes;
+        for (Basis *B : b->pinned) B->pins--;
+        delete b;
+        return (decaes_batch *)nullptr;
+    };
+    int launches = 0;
+    if (int rc = batch_plan(ctx, vols, nvol, ctx->stream, b->bp, &launches)) return bail(rc);
+    for (auto &bv : b->bp.vols) { bv.B->pins++; b->pinned.push_back(bv.B); }
+    size_t sz[5];
+    const size_t total = batch_bytes(b->bp, &sz[0], &sz[1], &sz[2], &sz[3], &sz[4]);
+    if (ctx->used + total > ctx->budget) {
+        fail(ctx, DECAES_ENOMEM, "the batch's working buffers (" + std::to_string(total) + " bytes) exceed the HBM budget");
+        return bail(DECAES_ENOMEM);
+    }
+    void *p[5];
+    for (int i = 0; i < 5; ++i) {
+        cudaError_t e = cudaMalloc(&p[i], sz[i]);
+        if (e != cudaSuccess) {
+            fail(ctx, DECAES_ECUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            return bail(DECAES_ECUDA);
+        }
+        b->owned.push_back(p[i]);
+        b->owned_bytes += sz[i];
+        ctx->used += sz[i];
+    }
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) { fail(ctx, DECAES_ECUDA, "basis preparation failed"); return bail(0); }
+    if (int rc = batch_bind(ctx, b->bp, p[0], p[1], p[2], p[3], p[4])) return bail(rc);
+    if (cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) != cudaSuccess) {
+        fail(ctx, DECAES_ECUDA, "cudaStreamCreate failed");
+        return bail(0);
+    }
+    if (cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        fail(ctx, DECAES_ECUDA, "cudaStreamBeginCapture failed");
+        return bail(0);
+    }
+    int rc = batch_enqueue(ctx, b->bp, b->cap, &b->launches);
+    cudaGraph_t g = nullptr;
+    cudaError_t ee = cudaStreamEndCapture(b->cap, &g);
+    b->graph = g;
+    if (rc || ee != cudaSuccess || !g) {
+        if (!rc) fail(ctx, DECAES_ECUDA, std::string("stream capture: ") + cudaGetErrorString(ee));
+        return bail(0);
+    }
+    cudaError_t ie = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (ie != cudaSuccess) {
+        fail(ctx, DECAES_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+        return bail(0);
+    }
+    return b;
+}
+
+extern "C" int decaes_batch_run(decaes_batch *b, void *stream) {
+    if (!b) return DECAES_EINVAL;
+    decaes_ctx *ctx = b->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    CK(cudaGraphLaunch(b->exec, st));
+    return DECAES_OK;
+}
+
+extern "C" void decaes_batch_destroy(decaes_batch *b) {
+    if (!b) return;
+    decaes_ctx *ctx = b->ctx;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->cap) cudaStreamDestroy(b->cap);
+    for (void *p : b->owned) cudaFree(p);
+    ctx->used -= b->owned_bytes;
+    for (Basis *B : b->pinned) B->pins--;
+    delete b;
+}
+
+extern "C" int decaes_autotune(decaes_ctx *ctx, const decaes_t2map_opts *opts, decaes_tuning *out) {
+    if (int rc = check_both(ctx, opts, nullptr, DECAES_F32)) return rc;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    decaes_t2map_opts o = *opts;
+    o.MatrixSize[0] = 96; o.MatrixSize[1] = 96; o.MatrixSize[2] = 1;
+    o.Threshold = 0.0;
+    o.SaveResidualNorm = o.SaveDecayCurve = o.SaveRegParam = o.SaveNNLSBasis = 0;
+    const long V = 96L * 96;
+    decaes_mock_opts mo{};
+    mo.MatrixSize[0] = 96; mo.MatrixSize[1] = 96; mo.MatrixSize[2] = 1;
+    mo.nTE = o.nTE; mo.TE = o.TE; mo.T1 = 1.0;
+    mo.FlipAngleRange[0] = 140; mo.FlipAngleRange[1] = 180;
+    mo.MyelinT2Range[0] = 15e-3; mo.MyelinT2Range[1] = 25e-3;
+    mo.MyelinFracRange[0] = 0.05; mo.MyelinFracRange[1] = 0.25;
+    mo.IET2Range[0] = 60e-3; mo.IET2Range[1] = 90e-3;
+    mo.CSFT2Range[0] = 1.0; mo.CSFT2Range[1] = 2.0;
+    mo.CSFFracRange[0] = 0.0; mo.CSFFracRange[1] = 0.05;
+    mo.AmplitudeRange[0] = 500; mo.AmplitudeRange[1] = 2000;
+    mo.SNRRange[0] = 50; mo.SNRRange[1] = 200;
+    mo.BackgroundFraction = 0.0; mo.BackgroundSigma = 8.0;
+    std::vector<float> img((size_t)V * o.nTE);
+    dh::mock_image(mo, 7, img.data(), DECAES_F32, 0);
+    void *d_img;
+    if (int rc = buf(ctx, "tune_image", sizeof(float) * img.size(), &d_img)) return rc;
+    CK(cudaMemcpy(d_img, img.data(), sizeof(float) * img.size(), cudaMemcpyHostToDevice));
+    OutMap om;
+    if (int rc = out_layout(ctx, o, false, om)) return rc;
+    const int cand[3] = {1, 2, 4};
+    int best_w = 1;
+    double best_ms = 1e30;
+    for (int w : cand) {
+        ctx->force_wpb = w;
+        float best = 1e30f;
+        for (int rep = 0; rep < 2; ++rep) {
+            int nl = 0;
+            int rc = run_t2map(ctx, o, nullptr, d_img, DECAES_F32, nullptr, om, ctx->stream, &nl);
+            if (rc) { ctx->force_wpb = 0; return rc; }
+            CK(cudaStreamSynchronize(ctx->stream));
+            float t = 0;
+            cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]);
+            if (rep > 0) best = std::min(best, t);  // first run warms the basis and the caches
+        }
+        if (best < best_ms) { best_ms = best; best_w = w; }
+    }
+    ctx->force_wpb = 0;
+    const bool fixed = !std::isnan(o.SetFlipAngle);
+    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, o.precision == DECAES_PREC_MIXED, o.RefConAngle == 180.0};
+    Tune t;
+    t.wpb = best_w;
+    t.us_per_voxel = best_ms * 1e3 / (double)V;
+    ctx->tune[k] = t;
+    if (out) { out->warps_per_block = t.wpb; out->us_per_voxel = t.us_per_voxel; }
     return DECAES_OK;
 }

@@ -39,6 +39,20 @@ struct Params {
     const double *Gs;   // packed Gram matrices A_k'A_k of the grid bases (K x n(n+1)/2), or of the fixed basis
     const double *AsT;  // the grid (or fixed) bases transposed, K x m x n (row-major per basis)
     int epg_lanes_f32;  // lanes of the FP32 EPG (states in the Gram and factor regions)
+    long smem_stride;   // doubles of shared memory per warp (several warps per block)
+};
+// Doubles a copy of Params occupies (batched launch: one copy per warp).
+constexpr int kParamsDoubles = (int)((sizeof(Params) + 7) / 8);
+
+// The batched launch: many volumes, one persistent kernel.
+struct BatchParams {
+    const Params *vols;   // per-volume parameters, in queue order (device)
+    const int *offsets;   // nvol + 1 prefix offsets of the compacted voxel lists
+    int nvol;
+    int *counter;         // queue position
+    double *scratch;
+    long scr_stride;      // doubles of global scratch per warp (maximum over volumes)
+    long smem_stride;     // doubles of shared memory per warp (Params copy + largest workspace)
 };
 
 // Shared-memory footprint of one warp worker (doubles), mirrored on the host.

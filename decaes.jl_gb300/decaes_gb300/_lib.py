@@ -57,10 +57,22 @@ class MockOptsC(C.Structure):
         ("BackgroundFraction", C.c_double), ("BackgroundSigma", C.c_double)]
 
 
+class VolumeC(C.Structure):
+    """decaes_volume: one volume of a batched launch (device pointers)."""
+    _fields_ = [("mopts", T2mapOptsC), ("popts", T2partOptsC), ("has_t2part", C.c_int32), ("dtype", C.c_int32),
+                ("d_image", _vp), ("d_b1map", _vp), ("d_mout", T2mapOutC), ("d_pout", T2partOutC)]
+
+
+class TuningC(C.Structure):
+    _fields_ = [("warps_per_block", C.c_int32), ("us_per_voxel", C.c_double)]
+
+
 # Every symbol include/decaes_gpu.h declares.
 EXPORTS = ["decaes_create", "decaes_destroy", "decaes_last_error", "decaes_get_stats", "decaes_t2map_check_options",
            "decaes_t2part_check_options", "decaes_t2map", "decaes_t2part", "decaes_t2map_t2part",
-           "decaes_t2map_t2part_device", "decaes_sync_stats", "decaes_mock_image", "decaes_t2map_t2part_noalloc"]
+           "decaes_t2map_t2part_device", "decaes_sync_stats", "decaes_mock_image", "decaes_t2map_t2part_noalloc",
+           "decaes_t2map_t2part_batch", "decaes_batch_create", "decaes_batch_run", "decaes_batch_destroy",
+           "decaes_autotune"]
 
 _lib = None
 
@@ -98,6 +110,12 @@ def load(build_if_needed: bool = True):
     L.decaes_mock_image.argtypes = [C.POINTER(MockOptsC), C.c_uint64, _vp, C.c_int, C.c_int]
     L.decaes_t2map_t2part_noalloc.argtypes = [C.POINTER(T2mapOptsC), C.POINTER(T2partOptsC), _vp, C.c_int, _vp,
                                               C.POINTER(T2mapOutC), C.POINTER(T2partOutC), _vp, C.c_char_p, C.c_size_t]
+    L.decaes_t2map_t2part_batch.argtypes = [_vp, C.POINTER(VolumeC), C.c_int32, _vp]
+    L.decaes_batch_create.argtypes = [_vp, C.POINTER(VolumeC), C.c_int32]
+    L.decaes_batch_create.restype = _vp
+    L.decaes_batch_run.argtypes = [_vp, _vp]
+    L.decaes_batch_destroy.argtypes = [_vp]
+    L.decaes_autotune.argtypes = [_vp, C.POINTER(T2mapOptsC), C.POINTER(TuningC)]
     _lib = L
     return L
 

@@ -159,6 +159,56 @@ int decaes_t2map_t2part_device(decaes_ctx *ctx, const decaes_t2map_opts *mopts, 
  * decaes_stats (processed voxels, cap hits, device times). */
 int decaes_sync_stats(decaes_ctx *ctx, void *stream);
 
+/* ---- batched volumes -------------------------------------------------------
+ * Many volumes, each with its own options (nTE, TE, nT2, regularizer, method,
+ * mask), solved by ONE persistent voxel-kernel launch: the compacted voxel
+ * lists of all volumes form one work queue, most expensive volume first (cost
+ * per voxel from the autotuner when it has seen the shape, else a model), so
+ * the end of the launch is made of cheap voxels.  No reference counterpart
+ * (the reference runs one volume per call); it serves uneven workloads and the
+ * serving loop.  All pointers are device addresses on the context's device;
+ * each volume's image and outputs are of its `dtype`; the per-call constant
+ * outputs (echotimes ... decaybasisset) must be NULL.  Results are identical
+ * to one decaes_t2map_t2part_device call per volume. */
+typedef struct {
+    decaes_t2map_opts mopts;
+    decaes_t2part_opts popts;  /* used when has_t2part != 0 */
+    int32_t has_t2part;
+    int32_t dtype;             /* DECAES_F32 or DECAES_F64 */
+    const void *d_image;
+    const void *d_b1map;       /* NULL: flip-angle search */
+    decaes_t2map_out d_mout;
+    decaes_t2part_out d_pout;
+} decaes_volume;
+
+/* Enqueues the batch on `stream` (NULL = the context's stream) and returns;
+ * synchronize the stream before reading outputs.  decaes_get_stats reports
+ * the number of kernel launches. */
+int decaes_t2map_t2part_batch(decaes_ctx *ctx, const decaes_volume *vols, int32_t nvol, void *stream);
+
+/* A batch prepared once and captured as a CUDA graph, for the same volumes
+ * (same buffers and options) processed repeatedly: create validates,
+ * allocates the batch's own working buffers, makes the bases resident (held
+ * until destroy) and captures the launch sequence; run replays it on
+ * `stream` (NULL = the context's stream).  create returns NULL on failure
+ * (message in decaes_last_error(ctx)).  A prepared batch must be destroyed
+ * before its context. */
+typedef struct decaes_batch decaes_batch;
+decaes_batch *decaes_batch_create(decaes_ctx *ctx, const decaes_volume *vols, int32_t nvol);
+int decaes_batch_run(decaes_batch *batch, void *stream);
+void decaes_batch_destroy(decaes_batch *batch);
+
+/* Autotuner: times the voxel kernel on a synthetic slab of the given shape
+ * and method with 1, 2 and 4 warps per block, keeps the fastest for that
+ * (nTE, nT2, nRefAngles, Reg, precision, control angle) in the context, and
+ * reports it.  Later calls on the context use the tuned shape; batches also
+ * use the measured cost to order their queue. */
+typedef struct {
+    int32_t warps_per_block;
+    double us_per_voxel;       /* device time per above-threshold voxel, whole GPU */
+} decaes_tuning;
+int decaes_autotune(decaes_ctx *ctx, const decaes_t2map_opts *opts, decaes_tuning *out);
+
 /* Fused T2mapSEcorr + T2partSEcorr that allocates no device memory.  This entry
  * point has no counterpart in the reference; it exists for callers that cannot
  * let a library allocate: a host with a fixed device-memory plan (a real-time
