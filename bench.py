@@ -274,6 +274,88 @@ class _Null:
         return False
 
 
+def run_batch_workload(args):
+    """The batched uneven workload: many volumes of different shapes solved by
+    one persistent launch (a prepared batch replayed as a CUDA graph), against
+    the same volumes solved one device call after another."""
+    import torch
+    import decaes_gb300 as D
+    from decaes_gb300 import _lib
+    rng = np.random.default_rng(args.seed)
+    nvol = args.nvol
+    vols, specs = [], []
+    V_tot = 0
+    for i in range(nvol):
+        X = (int(rng.choice(np.arange(64, 241, 16))), int(rng.choice(np.arange(64, 241, 16))), int(rng.integers(1, 4)))
+        m, n = int(rng.integers(24, 65)), int(rng.choice([40, 48, 60]))
+        TE, bg = float(rng.uniform(5e-3, 12e-3)), float(rng.uniform(0.3, 0.6))
+        reg = "chi2" if i % 2 == 0 else "none"
+        mo = D.T2mapOptions(MatrixSize=X, nTE=m, TE=TE, nT2=n, T2Range=(10e-3, 2.0), Reg=reg, nRefAngles=32,
+                            Chi2Factor=1.02 if reg == "chi2" else None, Threshold=THRESHOLD, precision=args.precision)
+        po = D.T2partOptions.from_t2map(mo, SPWin=SPWIN, MPWin=MPWIN)
+        img = D.mock_image(D.MockImageOptions(MatrixSize=X, nTE=m, TE=TE, BackgroundFraction=bg), seed=args.seed + i,
+                           dtype=np.float32)
+        d_img = torch.from_numpy(img.reshape(-1, order="F").copy()).cuda()
+        V = int(np.prod(X))
+        V_tot += V
+        out = {"dist": torch.empty(V * n, dtype=torch.float32, device="cuda")}
+        for k in ("gdn", "ggm", "gva", "fnr", "snr", "alpha", "sfr", "sgm", "mfr", "mgm"):
+            out[k] = torch.empty(V, dtype=torch.float32, device="cuda")
+        mc = _lib.T2mapOutC(**{k: out[k].data_ptr() for k in ("dist", "gdn", "ggm", "gva", "fnr", "snr", "alpha")})
+        pc = _lib.T2partOutC(**{k: out[k].data_ptr() for k in ("sfr", "sgm", "mfr", "mgm")})
+        vols.append(_lib.VolumeC(mopts=mo.to_c(), popts=po.to_c(), has_t2part=1, dtype=_lib.F32,
+                                 d_image=d_img.data_ptr(), d_b1map=None, d_mout=mc, d_pout=pc))
+        specs.append((mo, po, d_img, out, mc, pc))
+    ctx = D.Context(0)
+    L = ctx.L
+    arr = (_lib.VolumeC * nvol)(*vols)
+    b = L.decaes_batch_create(ctx.h, arr, nvol)
+    if not b:
+        raise RuntimeError(L.decaes_last_error(ctx.h).decode())
+    stream = torch.cuda.Stream()  # an explicit stream: the events below see exactly the batch's work
+    for _ in range(args.warmup):
+        L.decaes_batch_run(b, C.c_void_p(stream.cuda_stream))
+    torch.cuda.synchronize()
+    clk = Clocks(0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            L.decaes_batch_run(b, C.c_void_p(stream.cuda_stream))
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    sfr_batch = [sp[3]["sfr"].double().cpu().numpy() for sp in specs]
+    L.decaes_batch_destroy(b)
+    # the same volumes, one device call each
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for mo, po, d_img, out, mc, pc in specs:
+        ctx.check(L.decaes_t2map_t2part_device(ctx.h, C.byref(mo.to_c()), C.byref(po.to_c()), C.c_void_p(d_img.data_ptr()),
+                                               _lib.F32, None, C.byref(mc), C.byref(pc), C.c_void_p(stream.cuda_stream)))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_seq = e0.elapsed_time(e1)
+    same = all(np.array_equal(np.nan_to_num(a, nan=-1), np.nan_to_num(sp[3]["sfr"].double().cpu().numpy(), nan=-1))
+               for a, sp in zip(sfr_batch, specs))
+    line = {
+        "metric": f"voxels/s, {nvol} uneven volumes in one persistent launch (prepared batch, CUDA graph replay)",
+        "value": V_tot / (ms * 1e-3), "unit": "voxels/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f64+f32",
+        "data": "synthetic (seeded 3-compartment EPG + Rician noise per volume)",
+        "config": {"workload": f"{nvol} volumes: XY ~U{{64..240 step 16}}, Z ~U{{1..3}} (the z-extent of the "
+                               f"64x64x32..240x240x48 range scaled down to fit one bench step), nTE ~U{{24..64}}, "
+                               f"TE ~U(5,12) ms, nT2 in {{40,48,60}}, mask ~U(0.3,0.6), Reg alternating chi2/none, "
+                               f"32 angles, Float32, T2part fused",
+                   "precision": args.precision, "voxels": V_tot},
+        "sequential_device_calls": {"value": V_tot / (ms_seq * 1e-3), "ms": ms_seq,
+                                    "speedup_of_batch": ms_seq / ms, "same_outputs": bool(same)},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -284,7 +366,9 @@ def main():
                     help="method of the headline value; with mixed the FP64 method is measured beside it")
     ap.add_argument("--no-fp64-compare", action="store_true",
                     help="skip the FP64 comparison run of the mixed headline")
-    ap.add_argument("--workload", default="lcurve48", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="lcurve48", choices=sorted(WORKLOADS) + ["batch"],
+                    help="lcurve48 (headline), gcv56, or batch (uneven volumes in one launch)")
+    ap.add_argument("--nvol", type=int, default=256, help="volumes of --workload batch")
     ap.add_argument("--matrix", type=int, nargs=3, default=None, help="override the workload's MatrixSize")
     ap.add_argument("--compare-slices", type=int, default=None,
                     help="z-slices of the volume the FP64 comparison runs on (default: all for lcurve48, 2 for gcv56)")
@@ -296,7 +380,13 @@ def main():
     if args.cpu_sample is None:
         args.cpu_sample = 131072 if args.workload == "lcurve48" else 16384
     if args.impl == "reference":
+        if args.workload == "batch":
+            print(json.dumps({"impl": "reference", "unavailable": "the batched workload is this library's own "
+                              "multi-volume launch; the reference runs one volume per call"}), flush=True)
+            return
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch_workload(args)
 
     import torch
     import decaes_gb300 as D

@@ -394,11 +394,13 @@ int get_basis(decaes_ctx *ctx, const decaes_t2map_opts &o, Basis **out) {
         *out = &it->second;
         return DECAES_OK;
     }
-    if (ctx->bases.size() >= 8) {  // evict the least recently used key not held by a prepared batch
-        auto lru = ctx->bases.end();
+    // keep at most 8 keys resident, evicting the least recently used one that
+    // no batch holds (a batch may hold more; the HBM budget bounds them)
+    auto lru = ctx->bases.end();
+    if (ctx->bases.size() >= 8)
         for (auto i = ctx->bases.begin(); i != ctx->bases.end(); ++i)
             if (i->second.pins == 0 && (lru == ctx->bases.end() || i->second.last_use < lru->second.last_use)) lru = i;
-        if (lru == ctx->bases.end()) return fail(ctx, DECAES_ENOMEM, "all resident bases are held by prepared batches");
+    if (lru != ctx->bases.end()) {
         Basis &b = lru->second;
         cudaFree(b.t2); cudaFree(b.logt2); cudaFree(b.angles); cudaFree(b.As); cudaFree(b.dAs); cudaFree(b.fixed);
         cudaFree(b.Gs); cudaFree(b.AsT);
@@ -967,6 +969,11 @@ struct BatchVol {
 // named buffers (one-shot call) or allocations the prepared batch owns.
 struct BatchPrep {
     std::vector<BatchVol> vols;  // queue order: most expensive first
+    std::vector<Basis *> pinned;  // bases held by this batch
+    void unpin() {
+        for (Basis *B : pinned) B->pins--;
+        pinned.clear();
+    }
     size_t n_out = 0, n_vidx = 0, n_w = 0;
     double *outs = nullptr, *weights = nullptr, *scratch = nullptr;
     int *vidx = nullptr, *cnt = nullptr;  // cnt: counts[nvol], offsets[nvol + 1], counter
@@ -993,6 +1000,7 @@ double voxel_cost(decaes_ctx *ctx, const decaes_t2map_opts &o) {
 
 int batch_plan(decaes_ctx *ctx, const decaes_volume *vols, int nvol, cudaStream_t st, BatchPrep &bp, int *launches) {
     if (!vols || nvol < 1) return fail(ctx, DECAES_EINVAL, "a batch needs at least one volume");
+    bp.unpin();
     bp.vols.clear();
     for (int i = 0; i < nvol; ++i) {
         const decaes_volume &v = vols[i];
@@ -1009,6 +1017,8 @@ int batch_plan(decaes_ctx *ctx, const decaes_volume *vols, int nvol, cudaStream_
         bv.v = v;
         bv.t2part = po != nullptr;
         if (int rc = prepare_basis(ctx, v.mopts, st, &bv.B, launches)) return rc;
+        bv.B->pins++;  // held while the batch is planned (and, for a prepared batch, until it is destroyed)
+        bp.pinned.push_back(bv.B);
         if (po) {
             std::string e = dh::t2part_plan(*po, bv.pp);
             if (!e.empty()) return fail(ctx, DECAES_EINVAL, e);
@@ -1133,7 +1143,6 @@ struct decaes_batch {
     BatchPrep bp;
     std::vector<void *> owned;
     size_t owned_bytes = 0;
-    std::vector<Basis *> pinned;
     cudaStream_t cap = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1148,6 +1157,7 @@ extern "C" int decaes_t2map_t2part_batch(decaes_ctx *ctx, const decaes_volume *v
     int launches = 0;
     ctx->stats = decaes_stats{};
     BatchPrep bp;
+    struct Unpin { BatchPrep &b; ~Unpin() { b.unpin(); } } unpin{bp};
     if (int rc = batch_plan(ctx, vols, nvol, st, bp, &launches)) return rc;
     size_t b_out, b_vidx, b_w, b_par, b_scr;
     batch_bytes(bp, &b_out, &b_vidx, &b_w, &b_par, &b_scr);
@@ -1180,13 +1190,12 @@ extern "C" decaes_batch *decaes_batch_create(decaes_ctx *ctx, const decaes_volum
         if (b->cap) cudaStreamDestroy(b->cap);
         for (void *p : b->owned) cudaFree(p);
         ctx->used -= b->owned_bytes;
-        for (Basis *B : b->pinned) B->pins--;
+        b->bp.unpin();
         delete b;
         return (decaes_batch *)nullptr;
     };
     int launches = 0;
     if (int rc = batch_plan(ctx, vols, nvol, ctx->stream, b->bp, &launches)) return bail(rc);
-    for (auto &bv : b->bp.vols) { bv.B->pins++; b->pinned.push_back(bv.B); }
     size_t sz[5];
     const size_t total = batch_bytes(b->bp, &sz[0], &sz[1], &sz[2], &sz[3], &sz[4]);
     if (ctx->used + total > ctx->budget) {
@@ -1250,7 +1259,7 @@ extern "C" void decaes_batch_destroy(decaes_batch *b) {
     if (b->cap) cudaStreamDestroy(b->cap);
     for (void *p : b->owned) cudaFree(p);
     ctx->used -= b->owned_bytes;
-    for (Basis *B : b->pinned) B->pins--;
+    b->bp.unpin();
     delete b;
 }
 

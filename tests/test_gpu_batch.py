@@ -138,3 +138,20 @@ def test_batch_rejects_bad_volume(D, ctx):
     rc = D.load().decaes_t2map_t2part_batch(ctx.h, arr, 1, None)
     assert rc == 1
     assert b"constant outputs" in D.load().decaes_last_error(ctx.h)
+
+
+def test_batch_with_more_shapes_than_resident_bases(D, ctx):
+    """More distinct parameter keys than the context keeps resident (8): the
+    batch holds every basis it uses until it has run."""
+    import torch
+    cs = [dict(X=(3, 3, 1), m=24 + 2 * i, TE=10e-3, n=40, K=8, Reg="chi2", Chi2Factor=1.02,
+               prec="mixed" if i % 2 else "fp64", dtype=np.float32, seed=20 + i) for i in range(12)]
+    vols = [Vol(D, c) for c in cs]
+    arr = (_lib().VolumeC * len(vols))(*[v.volume_c() for v in vols])
+    ctx.check(D.load().decaes_t2map_t2part_batch(ctx.h, arr, len(vols), None))
+    ctx.check(D.load().decaes_sync_stats(ctx.h, None))
+    torch.cuda.synchronize()
+    got = [v.host() for v in vols]
+    for i, v in enumerate(vols):
+        v.reset()
+        _same(_single(D, ctx, v), got[i], f"vol{i}")
