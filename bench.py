@@ -36,6 +36,7 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "decaes.jl_gb300"))
+from decaes_gb300 import replicas  # noqa: E402  (pure Python; no library load)
 
 METRIC = "voxels/s T2map+T2part, 240×240×48×48 echoes: FP64 vs mixed prec @MWF|Δ|≤1e-3; p99"
 SPWIN, MPWIN = (10e-3, 25e-3), (25e-3, 200e-3)
@@ -242,8 +243,7 @@ class DeviceRun:
             self.step()
         torch.cuda.synchronize()
         self.stats()
-        if world > 1:
-            torch.distributed.barrier()
+        replicas.barrier(world)
         torch.cuda.synchronize()
         solve_ms, launches = [], 0
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -256,13 +256,8 @@ class DeviceRun:
                 launches += st["kernel_launches"]
             e1.record(self.stream)
             torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-            dist.barrier()
+        ms = replicas.max_over_ranks(e0.elapsed_time(e1), world, device="cuda")
+        replicas.barrier(world)
         return ms / steps, launches, solve_ms
 
 
@@ -392,9 +387,7 @@ def main():
     import decaes_gb300 as D
     from decaes_gb300 import _lib
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world, rank, local = replicas.rank_info()
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
@@ -403,7 +396,7 @@ def main():
     matrix = tuple(args.matrix) if args.matrix else WORKLOADS[args.workload]["matrix"]
     V = int(np.prod(matrix))
     mo, po, mock = workload(matrix, args.precision, args.workload)
-    img = D.mock_image(mock, seed=args.seed + rank, dtype=np.float32)
+    img = D.mock_image(mock, seed=replicas.replica_seed(args.seed, rank), dtype=np.float32)
     ctx = D.Context(local)
 
     # ---- headline method, device-resident ----
@@ -411,7 +404,7 @@ def main():
     clk = Clocks(local)
     ms_per_step, launches, solve_ms = run.timed(args.steps, args.warmup, world, clk)
     Vp = run.stats()["voxels_processed"]
-    value = world * V / (ms_per_step * 1e-3)
+    value = replicas.aggregate_voxels_per_s(V, ms_per_step, world)
     sfr_head = run.d_parts["sfr"].double().cpu().numpy()
 
     # ---- end to end through the host-buffer C ABI from pinned memory ----
