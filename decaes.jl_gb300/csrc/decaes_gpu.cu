@@ -8,12 +8,17 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -97,6 +102,22 @@ __global__ void k_fill(double *p, long len, double v) {
 // voxels are independent).
 __global__ void k_compact(const void *image, int f32, long V, double thr, int *vidx, int *nvox) {
     for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < V; v += (long)gridDim.x * blockDim.x) {
+        double b = f32 ? (double)static_cast<const float *>(image)[v] : static_cast<const double *>(image)[v];
+        bool keep = b > thr;
+        unsigned msk = __ballot_sync(__activemask(), keep);
+        if (keep) {
+            int leader = __ffs(msk) - 1, lane = threadIdx.x & 31, base = 0;
+            if (lane == leader) base = atomicAdd(nvox, __popc(msk));
+            base = __shfl_sync(msk, base, leader);
+            vidx[base + __popc(msk & ((1u << lane) - 1))] = (int)v;
+        }
+    }
+}
+
+// The same for the voxel range [v0, v1) of a volume (a chunk of a request in
+// the serving loop); voxel indices stay absolute.
+__global__ void k_compact_range(const void *image, int f32, long v0, long v1, double thr, int *vidx, int *nvox) {
+    for (long v = v0 + blockIdx.x * (long)blockDim.x + threadIdx.x; v < v1; v += (long)gridDim.x * blockDim.x) {
         double b = f32 ? (double)static_cast<const float *>(image)[v] : static_cast<const double *>(image)[v];
         bool keep = b > thr;
         unsigned msk = __ballot_sync(__activemask(), keep);
@@ -1317,4 +1338,443 @@ extern "C" int decaes_autotune(decaes_ctx *ctx, const decaes_t2map_opts *opts, d
     ctx->tune[k] = t;
     if (out) { out->warps_per_block = t.wpb; out->us_per_voxel = t.us_per_voxel; }
     return DECAES_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Serving loop: continuous batching of host requests
+// ---------------------------------------------------------------------------
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    int64_t id = 0;
+    decaes_t2map_opts mo{};
+    decaes_t2part_opts po{};
+    bool t2part = false;
+    const void *image = nullptr;
+    int dtype = DECAES_F64;
+    decaes_t2map_out mout{};
+    decaes_t2part_out pout{};
+    long V = 0;
+    size_t img_bytes = 0, out_len = 0, footprint = 0;
+    void *d_img = nullptr, *d_f32 = nullptr;
+    double *d_out = nullptr, *d_w = nullptr;
+    OutMap om{};
+    Basis *B = nullptr;
+    dh::T2partPlan pp{};
+    cudaEvent_t h2d = nullptr, d2h = nullptr;
+    long next_voxel = 0;  // first voxel not yet handed to a tick
+    int inflight = 0;     // chunks in the running tick
+    int state = 0;        // 0 queued, 1 admitted, 2 downloading, 3 done, 4 failed
+    bool charged = false; // footprint counted against the server's budget
+    int status = DECAES_OK;
+    Clock::time_point t_submit;
+};
+using ReqP = std::shared_ptr<Request>;
+
+struct Chunk {
+    ReqP r;
+    long v0, v1;
+    double cost;
+};
+
+}  // namespace
+
+struct decaes_server {
+    decaes_ctx *ctx = nullptr;
+    int64_t tick_voxels = 262144;
+    size_t budget = 0, used = 0;
+    cudaStream_t copy = nullptr, comp = nullptr;
+    cudaEvent_t tick_t0 = nullptr, tick_t1 = nullptr;
+    int cap_chunks = 2048;
+    dk::Params *d_params = nullptr, *h_params = nullptr;
+    int *d_cnt = nullptr, *d_vidx = nullptr;
+    unsigned long long *d_stats = nullptr;
+    double *d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    std::mutex mu;
+    std::condition_variable cv, cv_done;
+    std::deque<ReqP> queue;
+    std::vector<ReqP> active;
+    std::map<int64_t, ReqP> all;
+    int64_t next_id = 1;
+    bool stop = false;
+    std::thread th;
+    std::vector<double> lat_ms;
+    int64_t submitted = 0, completed = 0, failed = 0, voxels = 0, ticks = 0;
+    double busy_ms = 0;
+    Clock::time_point t0;
+};
+
+namespace {
+
+void srv_finish(decaes_server *S, const ReqP &r, int status) {
+    // called with S->mu held
+    if (r->d_img) cudaFreeAsync(r->d_img, S->copy);
+    if (r->d_out) cudaFreeAsync(r->d_out, S->copy);
+    if (r->d_f32) cudaFreeAsync(r->d_f32, S->copy);
+    if (r->d_w) cudaFreeAsync(r->d_w, S->copy);
+    r->d_img = r->d_f32 = nullptr;
+    r->d_out = r->d_w = nullptr;
+    if (r->h2d) cudaEventDestroy(r->h2d);
+    if (r->d2h) cudaEventDestroy(r->d2h);
+    r->h2d = r->d2h = nullptr;
+    if (r->B) { r->B->pins--; r->B = nullptr; }
+    if (r->charged) S->used -= r->footprint;
+    r->charged = false;
+    r->status = status;
+    r->state = status == DECAES_OK ? 3 : 4;
+    if (status == DECAES_OK) {
+        S->completed++;
+        S->voxels += r->V;
+        S->lat_ms.push_back(std::chrono::duration<double, std::milli>(Clock::now() - r->t_submit).count());
+    } else {
+        S->failed++;
+    }
+    S->active.erase(std::remove(S->active.begin(), S->active.end(), r), S->active.end());
+    S->cv_done.notify_all();
+}
+
+// Admits queued requests (FIFO) while their footprint fits: device buffers,
+// NaN-filled results, image upload on the copy stream.  S->mu held.
+void srv_admit(decaes_server *S) {
+    decaes_ctx *ctx = S->ctx;
+    while (!S->queue.empty()) {
+        ReqP r = S->queue.front();
+        if (r->footprint > S->budget) {
+            S->queue.pop_front();
+            S->active.push_back(r);
+            srv_finish(S, r, DECAES_ENOMEM);
+            continue;
+        }
+        if (S->used + r->footprint > S->budget) break;
+        S->queue.pop_front();
+        S->active.push_back(r);
+        S->used += r->footprint;
+        r->charged = true;
+        int nl = 0;
+        {
+            std::lock_guard<std::mutex> lk(ctx->mu);
+            if (prepare_basis(ctx, r->mo, ctx->stream, &r->B, &nl)) { srv_finish(S, r, DECAES_EINVAL); continue; }
+            r->B->pins++;
+        }
+        bool ok = cudaMallocAsync(&r->d_img, r->img_bytes, S->copy) == cudaSuccess &&
+                  cudaMallocAsync((void **)&r->d_out, sizeof(double) * r->out_len, S->copy) == cudaSuccess;
+        if (ok && r->dtype == DECAES_F32) ok = cudaMallocAsync(&r->d_f32, sizeof(float) * r->out_len, S->copy) == cudaSuccess;
+        if (ok && !r->pp.weights.empty()) {
+            ok = cudaMallocAsync((void **)&r->d_w, sizeof(double) * r->mo.nT2, S->copy) == cudaSuccess &&
+                 cudaMemcpyAsync(r->d_w, r->pp.weights.data(), sizeof(double) * r->mo.nT2, cudaMemcpyHostToDevice,
+                                 S->copy) == cudaSuccess;
+        }
+        if (ok) ok = cudaMemcpyAsync(r->d_img, r->image, r->img_bytes, cudaMemcpyHostToDevice, S->copy) == cudaSuccess;
+        if (ok) {
+            layout_outputs(r->mo, r->t2part, r->d_out, r->om);
+            int g = (int)std::min<long>(4L * ctx->sms * 8, (long)(r->out_len + 255) / 256);
+            dk::k_fill<<<std::max(g, 1), 256, 0, S->copy>>>(r->d_out, (long)r->out_len, NAN);
+            ok = cudaGetLastError() == cudaSuccess && cudaEventCreateWithFlags(&r->h2d, cudaEventDisableTiming) == cudaSuccess &&
+                 cudaEventRecord(r->h2d, S->copy) == cudaSuccess;
+        }
+        if (!ok) { srv_finish(S, r, DECAES_ECUDA); continue; }
+        r->state = 1;
+    }
+}
+
+// Requests whose results finished downloading.  S->mu held.
+void srv_retire(decaes_server *S) {
+    std::vector<ReqP> done;
+    for (auto &r : S->active)
+        if (r->state == 2 && cudaEventQuery(r->d2h) == cudaSuccess) done.push_back(r);
+    for (auto &r : done) {
+        {
+            std::lock_guard<std::mutex> lk(S->ctx->mu);
+            copy_constants(r->mo, r->B, &r->mout, r->dtype, S->ctx);
+        }
+        srv_finish(S, r, DECAES_OK);
+    }
+}
+
+// Downloads a finished request's results (after the tick that completed it).
+void srv_download(decaes_server *S, const ReqP &r) {
+    decaes_ctx *ctx = S->ctx;
+    cudaStreamWaitEvent(S->copy, S->tick_t1, 0);
+    const OutMap &om = r->om;
+    const size_t V = (size_t)r->V, n = r->mo.nT2, m = r->mo.nTE;
+    struct { const double *s; void *d; size_t len; } cp[] = {
+        {om.dist, r->mout.dist, V * n}, {om.gdn, r->mout.gdn, V}, {om.ggm, r->mout.ggm, V}, {om.gva, r->mout.gva, V},
+        {om.fnr, r->mout.fnr, V}, {om.snr, r->mout.snr, V}, {om.alpha, r->mout.alpha, V},
+        {om.resnorm, r->mout.resnorm, V}, {om.decaycurve, r->mout.decaycurve, V * m}, {om.mu, r->mout.mu, V},
+        {om.chi2f, r->mout.chi2factor, V}, {om.basis, r->mout.decaybasis, V * m * n},
+        {om.sfr, r->t2part ? r->pout.sfr : nullptr, V}, {om.sgm, r->t2part ? r->pout.sgm : nullptr, V},
+        {om.mfr, r->t2part ? r->pout.mfr : nullptr, V}, {om.mgm, r->t2part ? r->pout.mgm : nullptr, V},
+    };
+    bool ok = true;
+    for (auto &c : cp) {
+        if (!c.s || !c.d || !ok) continue;
+        if (r->dtype == DECAES_F64) {
+            ok = cudaMemcpyAsync(c.d, c.s, sizeof(double) * c.len, cudaMemcpyDeviceToHost, S->copy) == cudaSuccess;
+        } else {
+            float *tmp = (float *)r->d_f32 + (c.s - r->d_out);
+            int g = (int)std::min<long>(8L * ctx->sms, ((long)c.len + 255) / 256);
+            dk::k_narrow<<<std::max(g, 1), 256, 0, S->copy>>>(c.s, tmp, (long)c.len);
+            ok = cudaMemcpyAsync(c.d, tmp, sizeof(float) * c.len, cudaMemcpyDeviceToHost, S->copy) == cudaSuccess;
+        }
+    }
+    if (ok) ok = cudaEventCreateWithFlags(&r->d2h, cudaEventDisableTiming) == cudaSuccess &&
+                 cudaEventRecord(r->d2h, S->copy) == cudaSuccess;
+    if (!ok) { srv_finish(S, r, DECAES_ECUDA); return; }
+    r->state = 2;
+}
+
+// Builds and launches one tick (a batched launch over chunks of the admitted
+// requests, in arrival order).  Returns the chunks, empty if there was no work.
+std::vector<Chunk> srv_launch_tick(decaes_server *S) {
+    decaes_ctx *ctx = S->ctx;
+    std::vector<Chunk> ch;
+    long left = S->tick_voxels;
+    std::lock_guard<std::mutex> ctx_lock(ctx->mu);
+    for (auto &r : S->active) {
+        if (left <= 0 || (int)ch.size() >= S->cap_chunks) break;
+        if (r->state != 1 || r->next_voxel >= r->V) continue;
+        if (cudaEventQuery(r->h2d) != cudaSuccess) continue;  // still uploading: next tick
+        const long take = std::min(left, r->V - r->next_voxel);
+        ch.push_back(Chunk{r, r->next_voxel, r->next_voxel + take, voxel_cost(ctx, r->mo) * (double)take});
+        r->next_voxel += take;
+        r->inflight++;
+        left -= take;
+    }
+    if (ch.empty()) return ch;
+    std::stable_sort(ch.begin(), ch.end(), [](const Chunk &a, const Chunk &b) { return a.cost > b.cost; });
+    const int nq = (int)ch.size();
+    long smem_stride = 0, scr_stride = 0, voff = 0;
+    bool ok = true;
+    for (int q = 0; q < nq && ok; ++q) {
+        const Chunk &c = ch[q];
+        long wsm = 0;
+        ok = make_params(ctx, c.r->mo, c.r->t2part ? &c.r->pp : nullptr, c.r->d_w, c.r->B, c.r->d_img, c.r->dtype,
+                         nullptr, c.r->om, S->h_params[q], &wsm) == DECAES_OK;
+        S->h_params[q].vidx = S->d_vidx + voff;
+        S->h_params[q].nvox = S->d_cnt + q;
+        S->h_params[q].stats = S->d_stats + 2 * q;
+        voff += c.v1 - c.v0;
+        smem_stride = std::max(smem_stride, (long)dk::kParamsDoubles + wsm);
+        scr_stride = std::max(scr_stride, S->h_params[q].scr_stride);
+    }
+    smem_stride = (smem_stride + 1) & ~1L;
+    int wpb = 1, grid = 0;
+    size_t smem = 0;
+    if (ok) {
+        wpb = tuned_wpb(ctx, ch[0].r->mo);
+        ok = launch_shape(ctx, dk::k_voxels_batch, smem_stride, &wpb, &grid, &smem) == DECAES_OK;
+    }
+    const size_t need = sizeof(double) * (size_t)scr_stride * grid * wpb;
+    if (ok && need > S->scratch_bytes) {
+        if (S->d_scratch) cudaFreeAsync(S->d_scratch, S->comp);
+        S->d_scratch = nullptr;
+        ok = cudaMallocAsync((void **)&S->d_scratch, need, S->comp) == cudaSuccess;
+        S->scratch_bytes = ok ? need : 0;
+    }
+    cudaStream_t st = S->comp;
+    int *counts = S->d_cnt, *offsets = S->d_cnt + nq, *counter = S->d_cnt + 2 * nq + 1;
+    if (ok) ok = cudaMemcpyAsync(S->d_params, S->h_params, sizeof(dk::Params) * nq, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+                 cudaMemsetAsync(S->d_cnt, 0, sizeof(int) * (2 * nq + 2), st) == cudaSuccess &&
+                 cudaMemsetAsync(S->d_stats, 0, 16 * nq, st) == cudaSuccess;
+    if (ok) {
+        cudaEventRecord(S->tick_t0, st);
+        long vo = 0;
+        for (int q = 0; q < nq; ++q) {
+            const Chunk &c = ch[q];
+            cudaStreamWaitEvent(st, c.r->h2d, 0);
+            int g = (int)std::min<long>(8L * ctx->sms, (c.v1 - c.v0 + 255) / 256);
+            dk::k_compact_range<<<std::max(g, 1), 256, 0, st>>>(c.r->d_img, c.r->dtype == DECAES_F32, c.v0, c.v1,
+                                                                c.r->mo.Threshold, S->d_vidx + vo, counts + q);
+            vo += c.v1 - c.v0;
+        }
+        dk::k_batch_prefix<<<1, 32, 0, st>>>(counts, nq, offsets);
+        dk::BatchParams B{S->d_params, offsets, nq, counter, S->d_scratch, scr_stride, smem_stride};
+        dk::k_voxels_batch<<<grid, 32 * wpb, smem, st>>>(B);
+        ok = cudaGetLastError() == cudaSuccess && cudaEventRecord(S->tick_t1, st) == cudaSuccess;
+    }
+    if (!ok) {
+        cudaStreamSynchronize(S->comp);  // nothing of the failed tick may still read the requests' buffers
+        for (auto &c : ch) {
+            c.r->inflight--;
+            if (c.r->state == 1) srv_finish(S, c.r, DECAES_ECUDA);
+        }
+        ch.clear();
+    }
+    return ch;
+}
+
+void srv_loop(decaes_server *S) {
+    cudaSetDevice(S->ctx->device);
+    std::unique_lock<std::mutex> lk(S->mu);
+    for (;;) {
+        srv_admit(S);
+        srv_retire(S);
+        std::vector<Chunk> ch = srv_launch_tick(S);
+        if (!ch.empty()) {
+            S->ticks++;
+            // while the tick runs: admit (uploads overlap the solve) and retire downloads
+            while (cudaEventQuery(S->tick_t1) == cudaErrorNotReady) {
+                srv_admit(S);
+                srv_retire(S);
+                S->cv.wait_for(lk, std::chrono::microseconds(200));
+            }
+            float t = 0;
+            if (cudaEventElapsedTime(&t, S->tick_t0, S->tick_t1) == cudaSuccess) S->busy_ms += t;
+            const bool tick_ok = cudaEventQuery(S->tick_t1) == cudaSuccess;
+            for (auto &c : ch) {
+                c.r->inflight--;
+                if (c.r->state != 1) continue;
+                if (!tick_ok) { srv_finish(S, c.r, DECAES_ECUDA); continue; }
+                if (c.r->next_voxel >= c.r->V && c.r->inflight == 0) srv_download(S, c.r);
+            }
+            continue;
+        }
+        bool downloading = false;
+        for (auto &r : S->active) downloading |= r->state == 2;
+        if (S->stop && S->queue.empty() && S->active.empty()) break;
+        S->cv.wait_for(lk, std::chrono::microseconds(downloading || !S->active.empty() ? 200 : 2000));
+    }
+}
+
+}  // namespace
+
+extern "C" decaes_server *decaes_server_create(decaes_ctx *ctx, const decaes_server_opts *opts) {
+    if (!ctx) return nullptr;
+    auto *S = new decaes_server();
+    S->ctx = ctx;
+    if (opts && opts->tick_voxels > 0) S->tick_voxels = opts->tick_voxels;
+    S->budget = (opts && opts->hbm_budget_bytes) ? opts->hbm_budget_bytes : (size_t)160 << 30;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    bool ok = cudaStreamCreateWithFlags(&S->copy, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&S->comp, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreate(&S->tick_t0) == cudaSuccess && cudaEventCreate(&S->tick_t1) == cudaSuccess &&
+              cudaMalloc(&S->d_params, sizeof(dk::Params) * S->cap_chunks) == cudaSuccess &&
+              cudaMallocHost(&S->h_params, sizeof(dk::Params) * S->cap_chunks) == cudaSuccess &&
+              cudaMalloc(&S->d_cnt, sizeof(int) * (2 * S->cap_chunks + 2)) == cudaSuccess &&
+              cudaMalloc(&S->d_stats, 16 * S->cap_chunks) == cudaSuccess &&
+              cudaMalloc(&S->d_vidx, sizeof(int) * (size_t)S->tick_voxels) == cudaSuccess;
+    if (!ok) {
+        fail(ctx, DECAES_ECUDA, "server set-up failed");
+        if (S->d_params) cudaFree(S->d_params);
+        if (S->h_params) cudaFreeHost(S->h_params);
+        if (S->d_cnt) cudaFree(S->d_cnt);
+        if (S->d_stats) cudaFree(S->d_stats);
+        if (S->d_vidx) cudaFree(S->d_vidx);
+        if (S->copy) cudaStreamDestroy(S->copy);
+        if (S->comp) cudaStreamDestroy(S->comp);
+        delete S;
+        return nullptr;
+    }
+    S->t0 = Clock::now();
+    S->th = std::thread(srv_loop, S);
+    return S;
+}
+
+extern "C" int64_t decaes_server_submit(decaes_server *S, const decaes_t2map_opts *mopts, const decaes_t2part_opts *popts,
+                                        const void *image, int dtype, decaes_t2map_out *mout, decaes_t2part_out *pout) {
+    if (!S || !mopts || !image || !mout) return -DECAES_EINVAL;
+    if ((popts == nullptr) != (pout == nullptr)) return -DECAES_EINVAL;
+    decaes_ctx *ctx = S->ctx;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        if (int rc = check_both(ctx, mopts, popts, dtype)) return -rc;
+    }
+    auto r = std::make_shared<Request>();
+    r->mo = *mopts;
+    r->t2part = popts != nullptr;
+    if (popts) {
+        r->po = *popts;
+        std::string e = dh::t2part_plan(*popts, r->pp);
+        if (!e.empty()) { std::lock_guard<std::mutex> lk(ctx->mu); fail(ctx, DECAES_EINVAL, e); return -DECAES_EINVAL; }
+    }
+    r->image = image;
+    r->dtype = dtype;
+    r->mout = *mout;
+    if (pout) r->pout = *pout;
+    r->V = (long)mopts->MatrixSize[0] * mopts->MatrixSize[1] * mopts->MatrixSize[2];
+    r->img_bytes = esize(dtype) * (size_t)r->V * mopts->nTE;
+    OutMap tmp;
+    r->out_len = layout_outputs(r->mo, r->t2part, nullptr, tmp);
+    r->footprint = r->img_bytes + sizeof(double) * r->out_len + (dtype == DECAES_F32 ? sizeof(float) * r->out_len : 0) +
+                   sizeof(double) * mopts->nT2 + 4096;
+    r->t_submit = Clock::now();
+    std::lock_guard<std::mutex> lk(S->mu);
+    r->id = S->next_id++;
+    S->all[r->id] = r;
+    S->queue.push_back(r);
+    S->submitted++;
+    S->cv.notify_all();
+    return r->id;
+}
+
+extern "C" int decaes_server_poll(decaes_server *S, int64_t id) {
+    if (!S) return -DECAES_EINVAL;
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->all.find(id);
+    if (it == S->all.end()) return -DECAES_EINVAL;
+    const Request &r = *it->second;
+    if (r.state == 3) return 1;
+    if (r.state == 4) return -r.status;
+    return 0;
+}
+
+extern "C" int decaes_server_wait(decaes_server *S, int64_t id) {
+    if (!S) return DECAES_EINVAL;
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto it = S->all.find(id);
+    if (it == S->all.end()) return DECAES_EINVAL;
+    ReqP r = it->second;
+    S->cv_done.wait(lk, [&] { return r->state >= 3; });
+    return r->status;
+}
+
+extern "C" int decaes_server_get_stats(decaes_server *S, decaes_server_stats *out) {
+    if (!S || !out) return DECAES_EINVAL;
+    std::lock_guard<std::mutex> lk(S->mu);
+    decaes_server_stats st{};
+    st.submitted = S->submitted; st.completed = S->completed; st.failed = S->failed;
+    st.voxels = S->voxels; st.ticks = S->ticks; st.busy_ms = S->busy_ms;
+    st.wall_ms = std::chrono::duration<double, std::milli>(Clock::now() - S->t0).count();
+    if (!S->lat_ms.empty()) {
+        std::vector<double> l = S->lat_ms;
+        std::sort(l.begin(), l.end());
+        auto q = [&](double p) { return l[std::min(l.size() - 1, (size_t)std::floor(p * (l.size() - 1) + 0.5))]; };
+        st.p50_ms = q(0.50);
+        st.p99_ms = q(0.99);
+        st.max_ms = l.back();
+        double s = 0;
+        for (double v : l) s += v;
+        st.mean_ms = s / l.size();
+    }
+    *out = st;
+    return DECAES_OK;
+}
+
+extern "C" void decaes_server_destroy(decaes_server *S) {
+    if (!S) return;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stop = true;
+        S->cv.notify_all();
+    }
+    if (S->th.joinable()) S->th.join();
+    cudaSetDevice(S->ctx->device);
+    cudaStreamSynchronize(S->copy);
+    cudaStreamSynchronize(S->comp);
+    if (S->d_scratch) cudaFreeAsync(S->d_scratch, S->comp);
+    cudaStreamSynchronize(S->comp);
+    cudaFree(S->d_params);
+    cudaFreeHost(S->h_params);
+    cudaFree(S->d_cnt);
+    cudaFree(S->d_stats);
+    cudaFree(S->d_vidx);
+    cudaEventDestroy(S->tick_t0);
+    cudaEventDestroy(S->tick_t1);
+    cudaStreamDestroy(S->copy);
+    cudaStreamDestroy(S->comp);
+    delete S;
 }

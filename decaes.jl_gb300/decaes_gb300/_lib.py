@@ -67,12 +67,22 @@ class TuningC(C.Structure):
     _fields_ = [("warps_per_block", C.c_int32), ("us_per_voxel", C.c_double)]
 
 
+class ServerOptsC(C.Structure):
+    _fields_ = [("tick_voxels", C.c_int64), ("hbm_budget_bytes", C.c_size_t)]
+
+
+class ServerStatsC(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in ("submitted", "completed", "failed", "voxels", "ticks")] + [
+        (k, C.c_double) for k in ("p50_ms", "p99_ms", "mean_ms", "max_ms", "busy_ms", "wall_ms")]
+
+
 # Every symbol include/decaes_gpu.h declares.
 EXPORTS = ["decaes_create", "decaes_destroy", "decaes_last_error", "decaes_get_stats", "decaes_t2map_check_options",
            "decaes_t2part_check_options", "decaes_t2map", "decaes_t2part", "decaes_t2map_t2part",
            "decaes_t2map_t2part_device", "decaes_sync_stats", "decaes_mock_image", "decaes_t2map_t2part_noalloc",
            "decaes_t2map_t2part_batch", "decaes_batch_create", "decaes_batch_run", "decaes_batch_destroy",
-           "decaes_autotune"]
+           "decaes_autotune", "decaes_server_create", "decaes_server_submit", "decaes_server_poll",
+           "decaes_server_wait", "decaes_server_get_stats", "decaes_server_destroy"]
 
 _lib = None
 
@@ -116,6 +126,15 @@ def load(build_if_needed: bool = True):
     L.decaes_batch_run.argtypes = [_vp, _vp]
     L.decaes_batch_destroy.argtypes = [_vp]
     L.decaes_autotune.argtypes = [_vp, C.POINTER(T2mapOptsC), C.POINTER(TuningC)]
+    L.decaes_server_create.argtypes = [_vp, C.POINTER(ServerOptsC)]
+    L.decaes_server_create.restype = _vp
+    L.decaes_server_submit.argtypes = [_vp, C.POINTER(T2mapOptsC), C.POINTER(T2partOptsC), _vp, C.c_int,
+                                       C.POINTER(T2mapOutC), C.POINTER(T2partOutC)]
+    L.decaes_server_submit.restype = C.c_int64
+    L.decaes_server_poll.argtypes = [_vp, C.c_int64]
+    L.decaes_server_wait.argtypes = [_vp, C.c_int64]
+    L.decaes_server_get_stats.argtypes = [_vp, C.POINTER(ServerStatsC)]
+    L.decaes_server_destroy.argtypes = [_vp]
     _lib = L
     return L
 

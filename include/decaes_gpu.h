@@ -209,6 +209,44 @@ typedef struct {
 } decaes_tuning;
 int decaes_autotune(decaes_ctx *ctx, const decaes_t2map_opts *opts, decaes_tuning *out);
 
+/* ---- serving loop -----------------------------------------------------------
+ * A continuous-batching server on one context (the GPU counterpart of the
+ * reference's warm-process request loop, api/decaes_server.jl:69-131).
+ * decaes_server_submit queues a T2map (+ T2part) request on HOST buffers and
+ * returns at once; a scheduler thread admits queued requests while their
+ * device footprint fits the server's HBM budget (image, FP64 results, voxel
+ * list), uploads them on a copy stream, and runs "ticks": each tick solves up
+ * to `tick_voxels` voxels taken in arrival order from every admitted request
+ * as ONE batched persistent launch, so requests that arrive while the GPU is
+ * busy join the next tick and their uploads and downloads overlap the solve.
+ * Bases stay resident per parameter key.  Each result is identical to the
+ * same request run alone.  Pinned host buffers let copies overlap; pageable
+ * ones work but serialize the copies with the scheduler. */
+typedef struct decaes_server decaes_server;
+typedef struct {
+    int64_t tick_voxels;       /* voxels per tick (0: 262144) */
+    size_t hbm_budget_bytes;   /* admission budget for request buffers (0: 160 GiB) */
+} decaes_server_opts;
+typedef struct {
+    int64_t submitted, completed, failed;
+    int64_t voxels;            /* of completed requests */
+    int64_t ticks;
+    double p50_ms, p99_ms, mean_ms, max_ms;  /* submit-to-result latency of completed requests */
+    double busy_ms;            /* device time of the ticks */
+    double wall_ms;            /* since the server started */
+} decaes_server_stats;
+decaes_server *decaes_server_create(decaes_ctx *ctx, const decaes_server_opts *opts);
+/* Returns a request id > 0, or -DECAES_E* (options are validated here). */
+int64_t decaes_server_submit(decaes_server *srv, const decaes_t2map_opts *mopts, const decaes_t2part_opts *popts,
+                             const void *image, int dtype, decaes_t2map_out *mout, decaes_t2part_out *pout);
+/* 1 = done, 0 = pending, -DECAES_E* = failed or unknown id. */
+int decaes_server_poll(decaes_server *srv, int64_t id);
+/* Blocks until the request is done; returns DECAES_OK or its error code. */
+int decaes_server_wait(decaes_server *srv, int64_t id);
+int decaes_server_get_stats(decaes_server *srv, decaes_server_stats *out);
+/* Finishes every queued request, then stops the scheduler and frees the server. */
+void decaes_server_destroy(decaes_server *srv);
+
 /* Fused T2mapSEcorr + T2partSEcorr that allocates no device memory.  This entry
  * point has no counterpart in the reference; it exists for callers that cannot
  * let a library allocate: a host with a fixed device-memory plan (a real-time
