@@ -351,6 +351,80 @@ def run_batch_workload(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serve_workload(args):
+    """The serving mix: Poisson arrivals of single slices (70%, 240x240x1, 48
+    echoes), slabs (25%, 240x240x16, 48 echoes) and full volumes (5%,
+    240x240x48, 56 echoes), each followed by T2part, through the library's
+    continuous-batching server under a 160 GB admission budget; reports p50/p99
+    submit-to-result latency and voxels/s at each arrival rate."""
+    import threading as th
+    import decaes_gb300 as D
+    from decaes_gb300.server import Server
+    rng = np.random.default_rng(args.seed)
+    kinds = [("slice", (240, 240, 1), "lcurve48", 0.70), ("slab", (240, 240, 16), "lcurve48", 0.25),
+             ("volume", (240, 240, 48), "gcv56", 0.05)]
+    pool = {}
+    for name, X, wl, _ in kinds:
+        mo, po, mock = workload(X, args.precision, wl)
+        pool[name] = [(D.mock_image(mock, seed=args.seed + 17 * i, dtype=np.float32), mo, po)
+                      for i in range(4 if name == "slice" else 1)]
+    ctx = D.Context(0)
+    rates = [float(r) for r in args.rates.split(",")]
+    results = []
+    for rate in rates:
+        srv = Server(ctx, tick_voxels=args.tick_voxels, hbm_budget_bytes=160 << 30)
+        # warm the bases and the kernels
+        for name in pool:
+            srv.result(srv.submit(*pool[name][0]))
+        st0 = srv.stats()
+        ids, t_sub = [], []
+        picks = rng.choice(len(kinds), size=args.requests, p=[k[3] for k in kinds])
+        gaps = rng.exponential(1.0 / rate, size=args.requests)
+        t_start = time.perf_counter()
+
+        def submitter():
+            t = time.perf_counter()
+            for k, g in zip(picks, gaps):
+                t += g
+                dt = t - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                name = kinds[k][0]
+                img, mo, po = pool[name][int(rng.integers(len(pool[name])))]
+                ids.append((srv.submit(img, mo, po), name, int(np.prod(mo.MatrixSize))))
+
+        sub = th.Thread(target=submitter)
+        with Clocks(0) as clk:
+            sub.start()
+            sub.join()
+            for rid, _, _ in ids:
+                srv.result(rid)
+        wall = time.perf_counter() - t_start
+        st = srv.stats()
+        srv.close()
+        vox = sum(v for _, _, v in ids)
+        results.append({"rate_req_per_s": rate, "requests": len(ids),
+                        "mix": {n: sum(1 for _, nn, _ in ids if nn == n) for n, _, _, _ in kinds},
+                        "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+                        "max_ms": st["max_ms"], "voxels_per_s": vox / wall, "wall_s": wall,
+                        "ticks": st["ticks"] - st0["ticks"], "device_busy_frac": (st["busy_ms"] - st0["busy_ms"]) / (wall * 1e3),
+                        "clocks": clk.summary()})
+    best = max(results, key=lambda r: r["voxels_per_s"])
+    line = {
+        "metric": "serving: p50/p99 latency and voxels/s, Poisson mix of slices/slabs/volumes (T2map+T2part)",
+        "value": best["voxels_per_s"], "unit": "voxels/s", "n_gpus": 1, "steps": len(rates), "warmup": 1,
+        "ms_per_step": best["wall_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f64+f32",
+        "data": "synthetic (seeded 3-compartment EPG + Rician noise, 35% background)",
+        "config": {"workload": "70% 240x240x1 / 25% 240x240x16 (48 echoes, nT2=40, lcurve) / 5% 240x240x48 "
+                               "(56 echoes, nT2=60, GCV), Float32 host buffers, T2part fused, 160 GB admission "
+                               f"budget, {args.tick_voxels} voxels per tick",
+                   "precision": args.precision},
+        "rates": results,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,9 +435,12 @@ def main():
                     help="method of the headline value; with mixed the FP64 method is measured beside it")
     ap.add_argument("--no-fp64-compare", action="store_true",
                     help="skip the FP64 comparison run of the mixed headline")
-    ap.add_argument("--workload", default="lcurve48", choices=sorted(WORKLOADS) + ["batch"],
-                    help="lcurve48 (headline), gcv56, or batch (uneven volumes in one launch)")
+    ap.add_argument("--workload", default="lcurve48", choices=sorted(WORKLOADS) + ["batch", "serve"],
+                    help="lcurve48 (headline), gcv56, batch (uneven volumes in one launch), serve (serving mix)")
     ap.add_argument("--nvol", type=int, default=256, help="volumes of --workload batch")
+    ap.add_argument("--rates", default="0.5,1,2", help="arrival rates (requests/s) of --workload serve")
+    ap.add_argument("--requests", type=int, default=40, help="requests per rate of --workload serve")
+    ap.add_argument("--tick-voxels", type=int, default=262144, help="voxels per server tick (--workload serve)")
     ap.add_argument("--matrix", type=int, nargs=3, default=None, help="override the workload's MatrixSize")
     ap.add_argument("--compare-slices", type=int, default=None,
                     help="z-slices of the volume the FP64 comparison runs on (default: all for lcurve48, 2 for gcv56)")
@@ -375,13 +452,15 @@ def main():
     if args.cpu_sample is None:
         args.cpu_sample = 131072 if args.workload == "lcurve48" else 16384
     if args.impl == "reference":
-        if args.workload == "batch":
+        if args.workload in ("batch", "serve"):
             print(json.dumps({"impl": "reference", "unavailable": "the batched workload is this library's own "
                               "multi-volume launch; the reference runs one volume per call"}), flush=True)
             return
         return run_reference(args)
     if args.workload == "batch":
         return run_batch_workload(args)
+    if args.workload == "serve":
+        return run_serve_workload(args)
 
     import torch
     import decaes_gb300 as D

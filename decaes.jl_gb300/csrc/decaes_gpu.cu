@@ -1533,15 +1533,35 @@ std::vector<Chunk> srv_launch_tick(decaes_server *S) {
     std::vector<Chunk> ch;
     long left = S->tick_voxels;
     std::lock_guard<std::mutex> ctx_lock(ctx->mu);
+    // eligible requests (uploaded, voxels left), in arrival order
+    std::vector<ReqP> el;
     for (auto &r : S->active) {
-        if (left <= 0 || (int)ch.size() >= S->cap_chunks) break;
+        if ((int)el.size() >= S->cap_chunks) break;
         if (r->state != 1 || r->next_voxel >= r->V) continue;
         if (cudaEventQuery(r->h2d) != cudaSuccess) continue;  // still uploading: next tick
-        const long take = std::min(left, r->V - r->next_voxel);
-        ch.push_back(Chunk{r, r->next_voxel, r->next_voxel + take, voxel_cost(ctx, r->mo) * (double)take});
-        r->next_voxel += take;
+        el.push_back(r);
+    }
+    if (el.empty()) return ch;
+    // fair share first (a large request cannot hold back the small ones that
+    // arrived after it), then what is left in arrival order; each request
+    // still contributes one contiguous chunk
+    std::vector<long> take(el.size(), 0);
+    const long share = std::max<long>(left / (long)el.size(), 1024);
+    for (size_t i = 0; i < el.size() && left > 0; ++i) {
+        take[i] = std::min({share, left, el[i]->V - el[i]->next_voxel});
+        left -= take[i];
+    }
+    for (size_t i = 0; i < el.size() && left > 0; ++i) {
+        const long more = std::min(left, el[i]->V - el[i]->next_voxel - take[i]);
+        take[i] += more;
+        left -= more;
+    }
+    for (size_t i = 0; i < el.size(); ++i) {
+        if (take[i] <= 0) continue;
+        ReqP &r = el[i];
+        ch.push_back(Chunk{r, r->next_voxel, r->next_voxel + take[i], voxel_cost(ctx, r->mo) * (double)take[i]});
+        r->next_voxel += take[i];
         r->inflight++;
-        left -= take;
     }
     if (ch.empty()) return ch;
     std::stable_sort(ch.begin(), ch.end(), [](const Chunk &a, const Chunk &b) { return a.cost > b.cost; });

@@ -216,9 +216,11 @@ int decaes_autotune(decaes_ctx *ctx, const decaes_t2map_opts *opts, decaes_tunin
  * returns at once; a scheduler thread admits queued requests while their
  * device footprint fits the server's HBM budget (image, FP64 results, voxel
  * list), uploads them on a copy stream, and runs "ticks": each tick solves up
- * to `tick_voxels` voxels taken in arrival order from every admitted request
- * as ONE batched persistent launch, so requests that arrive while the GPU is
- * busy join the next tick and their uploads and downloads overlap the solve.
+ * to `tick_voxels` voxels from every admitted request -- an equal share each
+ * first, then the remainder in arrival order -- as ONE batched persistent
+ * launch, so requests that arrive while the GPU is busy join the next tick
+ * (a large volume does not hold back the slices behind it) and their uploads
+ * and downloads overlap the solve.
  * Bases stay resident per parameter key.  Each result is identical to the
  * same request run alone.  Pinned host buffers let copies overlap; pageable
  * ones work but serialize the copies with the scheduler. */
