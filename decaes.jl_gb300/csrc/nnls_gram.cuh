@@ -75,10 +75,12 @@ __device__ __forceinline__ void warp_keymin(long long &key, int &j) {
     }
 }
 
-// 1/d for 1e-30 < d < 1e30: FP32 reciprocal (24 bits) refined by one cubic
-// Newton step r(1 + e + e^2), e = 1 - d r (error ~ e^3, below FP64 rounding).
+// 1/d for normal d: the hardware's approximate FP64 reciprocal (rcp.approx,
+// relative error below 2^-20) refined by one cubic Newton step
+// r(1 + e + e^2), e = 1 - d r, whose error e^3 is below FP64 rounding.
 __device__ __forceinline__ double fast_rcp(double d) {
-    const double r = (double)__frcp_rn((float)d);
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
     const double e = fma(-d, r, 1.0);
     return fma(r, fma(e, e, e), r);
 }
@@ -86,6 +88,18 @@ __device__ __forceinline__ double fast_rcp(double d) {
 __device__ __forceinline__ double lane_pick(double v0, double v1, int i) {
     // value held for row i (rows i < 32 in v0, rows >= 32 in v1) broadcast from its lane
     return __shfl_sync(FULL, i < 32 ? v0 : v1, i & 31);
+}
+
+// An FP32 value as FP64 by moving its exponent and mantissa fields (integer
+// pipes; exact for zero and normal numbers, the only values an EPG curve takes
+// here).
+__device__ __forceinline__ double widen(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned long long sgn = (unsigned long long)(u >> 31) << 63;
+    const unsigned long long mag = e == 0 ? 0ull
+                                          : ((unsigned long long)(e + (1023 - 127)) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)(sgn | mag));
 }
 
 // b'b.
@@ -131,10 +145,10 @@ __device__ __noinline__ void gram_build_f32(GramWS &g, const float *As, int lda,
         int i = 0;
         #pragma unroll 1
         for (; i + 1 < m; i += 2) {
-            s0 = fma((double)aj[i], b[i], s0);
-            s1 = fma((double)aj[i + 1], b[i + 1], s1);
+            s0 = fma(widen(aj[i]), b[i], s0);
+            s1 = fma(widen(aj[i + 1]), b[i + 1], s1);
         }
-        if (i < m) s0 = fma((double)aj[i], b[i], s0);
+        if (i < m) s0 = fma(widen(aj[i]), b[i], s0);
         g.f[j] = s0 + s1;
     }
     gram_bb(g, m, b);
@@ -150,10 +164,10 @@ __device__ __noinline__ void gram_build_f32(GramWS &g, const float *As, int lda,
         int r = 0;
         #pragma unroll 1
         for (; r + 1 < m; r += 2) {
-            s0 = fma((double)ai[r], (double)aj[r], s0);
-            s1 = fma((double)ai[r + 1], (double)aj[r + 1], s1);
+            s0 = fma(widen(ai[r]), widen(aj[r]), s0);
+            s1 = fma(widen(ai[r + 1]), widen(aj[r + 1]), s1);
         }
-        if (r < m) s0 = fma((double)ai[r], (double)aj[r], s0);
+        if (r < m) s0 = fma(widen(ai[r]), widen(aj[r]), s0);
         g.G[p] = s0 + s1;
     }
     __syncwarp();
@@ -168,14 +182,18 @@ __device__ __noinline__ void gram_load(GramWS &g, const double *Gg, int n) {
     __syncwarp();
 }
 
-// LDL' factorization of H_PP = G_PP + mu2 I from scratch (right-looking,
-// lanes over rows), then y = L^{-1} f_P.  Returns false when a pivot is not
+// LDL' factorization of H_PP = G_PP + mu2 I from scratch (right-looking),
+// with y = L^{-1} f_P carried along as an extra column.  Per pivot: one
+// reciprocal, the column scaled by the lanes of its rows, and the trailing
+// update spread over lanes by (row, column) pair, so a step costs ~(k-j)^2/64
+// FMA instructions instead of k-j.  Returns false when a pivot is not
 // positive relative to its diagonal (numerically dependent set).
 __device__ bool gram_refactor(GramWS &g, int k, double mu2) {
     const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;
     const int p0 = r0 < k ? g.P[r0] : 0, p1 = r1 < k ? g.P[r1] : 0;
     double *L0 = g.L + tri(r0 - 1), *L1 = g.L + tri(r1 - 1);
+    double *cu = g.xp;  // unscaled pivot column of the current step
     // strictly lower triangle and diagonal of H_PP, one row per lane
     if (r0 < k) {
         #pragma unroll 1
@@ -187,6 +205,7 @@ __device__ bool gram_refactor(GramWS &g, int k, double mu2) {
         for (int c = 0; c < r1; ++c) L1[c] = g.G[gidx(p1, g.P[c])];
         g.dd[r1] = g.G[tri(p1) + p1] + mu2;
     }
+    double v0 = r0 < k ? g.f[p0] : 0.0, v1 = r1 < k ? g.f[p1] : 0.0;
     __syncwarp();
     #pragma unroll 1
     for (int j = 0; j < k; ++j) {
@@ -195,33 +214,35 @@ __device__ bool gram_refactor(GramWS &g, int k, double mu2) {
         const double h = g.G[tri(pj) + pj] + mu2;
         if (!(d > kGramDepTol * h)) return false;
         const double rd = fast_rcp(d);
-        double c0 = 0.0, c1 = 0.0, l0 = 0.0, l1 = 0.0;
-        if (r0 > j && r0 < k) { c0 = L0[j]; l0 = c0 * rd; L0[j] = l0; }
-        if (r1 > j && r1 < k) { c1 = L1[j]; l1 = c1 * rd; L1[j] = l1; }
-        if (lane == 0) g.dinv[j] = rd;
-        __syncwarp();
-        // trailing update of row r: columns j < c < r, and the diagonal
+        const double yj = lane_pick(v0, v1, j);
         if (r0 > j && r0 < k) {
-            int bc = tri(j);  // start of row c = j + 1
-            #pragma unroll 1
-            for (int c = j + 1; c < r0; ++c) { L0[c] = fma(-c0, g.L[bc + j], L0[c]); bc += c; }
+            const double c0 = L0[j], l0 = c0 * rd;
+            L0[j] = l0;
+            cu[r0] = c0;
             g.dd[r0] = fma(-c0, l0, g.dd[r0]);
+            v0 = fma(-l0, yj, v0);
         }
         if (r1 > j && r1 < k) {
-            int bc = tri(j);
-            #pragma unroll 1
-            for (int c = j + 1; c < r1; ++c) { L1[c] = fma(-c1, g.L[bc + j], L1[c]); bc += c; }
+            const double c1 = L1[j], l1 = c1 * rd;
+            L1[j] = l1;
+            cu[r1] = c1;
             g.dd[r1] = fma(-c1, l1, g.dd[r1]);
+            v1 = fma(-l1, yj, v1);
+        }
+        if (lane == 0) g.dinv[j] = rd;
+        __syncwarp();
+        // trailing strictly-lower entries (r, c), j < c < r < k, one per lane
+        const int t = k - 1 - j, npair = t * (t - 1) / 2;
+        #pragma unroll 1
+        for (int q = lane; q < npair; q += 32) {
+            int a = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)q)) * 0.5f);
+            while (a * (a - 1) / 2 > q) --a;
+            while ((a + 1) * a / 2 <= q) ++a;
+            const int r = j + 1 + a, c = j + 1 + (q - a * (a - 1) / 2);
+            double *Lr = g.L + tri(r - 1);
+            Lr[c] = fma(-cu[r], g.L[tri(c - 1) + j], Lr[c]);
         }
         __syncwarp();
-    }
-    // y = L^{-1} f_P (unit lower, column-oriented)
-    double v0 = r0 < k ? g.f[p0] : 0.0, v1 = r1 < k ? g.f[p1] : 0.0;
-    #pragma unroll 1
-    for (int i = 0; i < k; ++i) {
-        const double ui = lane_pick(v0, v1, i);
-        if (r0 > i && r0 < k) v0 = fma(-L0[i], ui, v0);
-        if (r1 > i && r1 < k) v1 = fma(-L1[i], ui, v1);
     }
     if (r0 < k) g.y[r0] = v0;
     if (r1 < k) g.y[r1] = v1;
@@ -431,12 +452,12 @@ __device__ __noinline__ void gram_svdvals(GramWS g, double *W, int m, int n, dou
 }
 
 // NNLS on H = G + mu2 I with right-hand side f (prepared by gram_rhs_t /
-// gram_build_f32 / gram_load).  On return x (dense, n) holds the solution, idx
-// its passive columns (1-based, nsetp entries) and rnorm^2 = ||A x - b||^2 +
-// mu2 ||x||^2 with the residual formed explicitly from A (column-major m x n,
-// global).  mode = 1 when max_iter was reached (the reference's cap 3n).
-__device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double *wv, int *idx, const double *A, int m, int n,
-                                             const double *b, double mu2, int max_iter, int *lastk_io) {
+// gram_build_f32 / gram_load, which also set b'b).  On return x (dense, n)
+// holds the solution, idx its passive columns (1-based, nsetp entries) and
+// rnorm^2 = ||A x - b||^2 + mu2 ||x||^2.  mode = 1 when max_iter was reached
+// (the reference's cap 3n).
+__device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double *wv, int *idx, int n, double mu2,
+                                             int max_iter, int *lastk_io) {
     const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;
     #pragma unroll 1
@@ -600,24 +621,18 @@ __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double *wv, in
     #pragma unroll 1
     for (int r = lane; r < k; r += 32) g.xp[r] = x[g.P[r]];
     __syncwarp();
-    double res = 0.0, xx = 0.0;
+    // ||A x - b||^2 = b'b - f'x - mu^2 ||x||^2 at the solution ((G + mu^2 I)_PP x_P
+    // = f_P); the cancellation costs ~eps * b'b, far below the noise floor
+    double fx = 0.0, xx = 0.0;
     #pragma unroll 1
-    for (int i = lane; i < m; i += 32) {
-        double ri = b[i], ri2 = 0.0;
-        int r = 0;
-        #pragma unroll 1
-        for (; r + 1 < k; r += 2) {
-            ri = fma(-A[i + (long)m * g.P[r]], g.xp[r], ri);
-            ri2 = fma(-A[i + (long)m * g.P[r + 1]], g.xp[r + 1], ri2);
-        }
-        if (r < k) ri = fma(-A[i + (long)m * g.P[r]], g.xp[r], ri);
-        ri += ri2;
-        res = fma(ri, ri, res);
+    for (int r = lane; r < k; r += 32) {
+        const double xr = g.xp[r];
+        fx = fma(g.f[g.P[r]], xr, fx);
+        xx = fma(xr, xr, xx);
     }
-    #pragma unroll 1
-    for (int r = lane; r < k; r += 32) xx = fma(g.xp[r], g.xp[r], xx);
-    res = wsum(res);
+    fx = wsum(fx);
     xx = wsum(xx);
+    const double res = fmax(g.bb - fx - mu2 * xx, 0.0);
     NnlsResult out;
     out.nsetp = k;
     out.mode = mode;

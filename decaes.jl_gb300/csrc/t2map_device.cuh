@@ -36,7 +36,7 @@ __device__ __forceinline__ void note(Warp &w, const NnlsResult &r) { w.nnls_caps
 __device__ NnlsResult basis_lsq(Warp &w, bool tikh, double mu) {
     const Params &P = *w.P;
     if (w.mixed)
-        return gram_nnls(w.g, w.s.x, w.s.w, w.s.idx, w.A, P.m, P.n, w.data, tikh ? mu * mu : 0.0, 3 * P.n, &w.g.lastk);
+        return gram_nnls(w.g, w.s.x, w.s.w, w.s.idx, P.n, tikh ? mu * mu : 0.0, 3 * P.n, &w.g.lastk);
     return warp_lsq(w.s, w.A, P.m, P.n, w.data, tikh, mu);
 }
 
@@ -424,6 +424,16 @@ __device__ double menger(double j0, double j1, double k0, double k1, double l0, 
     double cr = __dsub_rn(__dmul_rn(djk0, dkl1), __dmul_rn(djk1, dkl0));
     return 2 * cr / sqrt(__dmul_rn(__dmul_rn(a, b), c));
 }
+// The mixed method's forms of the same tests: squared distances against
+// squared tolerances, and the curvature with one reciprocal square root (no
+// correctly rounded square roots and divisions on its dependency chain).
+__device__ __forceinline__ double sq2(double a, double b) { return fma(a, a, b * b); }
+__device__ double menger_fast(double j0, double j1, double k0, double k1, double l0, double l1) {
+    double djk0 = j0 - k0, djk1 = j1 - k1, dkl0 = k0 - l0, dkl1 = k1 - l1, dlj0 = l0 - j0, dlj1 = l1 - j1;
+    double a = sq2(djk0, djk1), b = sq2(dkl0, dkl1), c = sq2(dlj0, dlj1);
+    double cr = fma(djk0, dkl1, -(djk1 * dkl0));
+    return 2 * cr * rsqrt(a * b * c);
+}
 struct LcState {
     double x[4], P[8];
 };
@@ -436,7 +446,9 @@ __device__ void lc_update_curvature(LCurve &L, const LcState &s, const double *P
     for (int q = 0; q < 4; ++q) {
         double x = s.x[q], P0 = s.P[2 * q], P1 = s.P[2 * q + 1];
         double C = -CUDART_INF;
-        if (jmin(nrm2(P0 - Ptl[0], P1 - Ptl[1]), nrm2(P0 - Pbr[0], P1 - Pbr[1])) > Ctol) {
+        const bool far = L.w->mixed ? fmin(sq2(P0 - Ptl[0], P1 - Ptl[1]), sq2(P0 - Pbr[0], P1 - Pbr[1])) > Ctol * Ctol
+                                    : jmin(nrm2(P0 - Ptl[0], P1 - Ptl[1]), nrm2(P0 - Pbr[0], P1 - Pbr[1])) > Ctol;
+        if (far) {
             const long long kx = okey(x);
             long long km = 0, kp = 0;
             int im = -1, ip = -1;
@@ -459,7 +471,7 @@ __device__ void lc_update_curvature(LCurve &L, const LcState &s, const double *P
             double m0 = P0, m1 = P1, p0 = P0, p1 = P1;
             if (im >= 0) { m0 = L.pP[2 * im]; m1 = L.pP[2 * im + 1]; }
             if (ip >= 0) { p0 = L.pP[2 * ip]; p1 = L.pP[2 * ip + 1]; }
-            C = menger(m0, m1, P0, P1, p0, p1);
+            C = L.w->mixed ? menger_fast(m0, m1, P0, P1, p0, p1) : menger(m0, m1, P0, P1, p0, p1);
         }
         pc_set(L, x, P0, P1, C, false);
     }
@@ -517,7 +529,9 @@ __device__ double lcurve_corner(LCurve &L, double xlow, double xhigh, double xto
     double Ptl[2] = {st.P[0], st.P[1]}, Pbr[2] = {st.P[6], st.P[7]};
     lc_update_curvature(L, st, Ptl, Pbr, Ctol);
     int iter = 0;
-    while (!(fabs(st.x[3] - st.x[0]) < xtol || nrm2(st.P[0] - st.P[6], st.P[1] - st.P[7]) < Ptol)) {
+    const bool mixed = L.w->mixed;
+    while (!(fabs(st.x[3] - st.x[0]) < xtol || (mixed ? sq2(st.P[0] - st.P[6], st.P[1] - st.P[7]) < Ptol * Ptol
+                                                      : nrm2(st.P[0] - st.P[6], st.P[1] - st.P[7]) < Ptol))) {
         iter += 1;
         if (iter > kLoopCap || L.overflow) { L.w->loop_caps++; break; }
         double xb = L.px[pc_argmax(L)];
@@ -728,7 +742,7 @@ __device__ void fa_update(Search &S, int I) {
         // precomputed Gram matrix of grid basis I; A'b from its transposed copy
         gram_load(w.g, P.Gs + (long)(I - 1) * (n * (n + 1) / 2), n);
         gram_rhs_t(w.g, P.AsT + (long)(I - 1) * m * n, m, n, w.data);
-        r = gram_nnls(w.g, w.s.x, w.s.w, w.s.idx, A, m, n, w.data, 0.0, 3 * n, &w.g.lastk);
+        r = gram_nnls(w.g, w.s.x, w.s.w, w.s.idx, n, 0.0, 3 * n, &w.g.lastk);
     } else {
         r = warp_lsq(w.s, A, m, n, w.data, false, 0.0);
     }
@@ -930,13 +944,15 @@ __device__ void warp_basis(Warp &w, double alpha, double *out /* m x n, global *
 
 // Mixed method: the same curves with the recursion in FP32 (coefficients in
 // FP64, rounded once), states in the Gram and factor regions, curves written
-// to w.A (global), rounded to FP32 values and staged in w.As32.  The basis of
-// the voxel is then exactly these FP32 values, for the Gram matrix, the
-// residuals and the fitted curve alike.
+// as FP32 to the warp's global scratch, then staged in w.As32 and widened
+// (exactly, on the integer pipes) into w.A.  The basis of the voxel is these
+// FP32 values, for the Gram matrix and the fitted curve alike, and no FP32 <->
+// FP64 conversion occupies the FP64 pipe.
 __device__ void warp_basis_f32(Warp &w, double alpha) {
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lanes = P.epg_lanes_f32, lane = w.lane;
     float *S = reinterpret_cast<float *>(w.g.G);  // 3*m*lanes floats, lane-contiguous
+    float *Af = reinterpret_cast<float *>(w.scr + warp_scratch_f32_offset(m, n, P.K));
     #pragma unroll 1
     for (int j0 = 0; j0 < n; j0 += lanes) {
         int j = j0 + lane;
@@ -944,10 +960,10 @@ __device__ void warp_basis_f32(Warp &w, double alpha) {
             float *Sl = S + lane;
             if (P.beta180) {
                 dx::FlatCoef<float> q = dx::to_f32(dx::flat_coef(alpha, P.TE, P.t2[j], P.T1));
-                dx::epg_flat_inplace(m, q, Sl, lanes, w.A + (long)j * m, 1);
+                dx::epg_flat_inplace(m, q, Sl, lanes, Af + (long)j * m, 1);
             } else {
                 dx::VecCoef<float> q = dx::to_f32(dx::vec_coef(alpha, P.TE, P.t2[j], P.T1, P.beta));
-                dx::epg_vec_inplace(m, q, Sl, lanes, w.A + (long)j * m, 1);
+                dx::epg_vec_inplace(m, q, Sl, lanes, Af + (long)j * m, 1);
             }
         }
         __syncwarp();
@@ -957,8 +973,8 @@ __device__ void warp_basis_f32(Warp &w, double alpha) {
     #pragma unroll 1
     for (long q = lane; q < (long)m * n; q += 32) {
         const int i = (int)(q % m), j = (int)(q / m);
-        const float v = (float)w.A[q];
-        w.A[q] = (double)v;
+        const float v = Af[q];
+        w.A[q] = widen(v);
         w.As32[i + w.ldA * j] = v;
     }
     __threadfence_block();

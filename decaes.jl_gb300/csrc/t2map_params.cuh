@@ -83,9 +83,15 @@ __host__ __device__ inline long warp_smem_doubles_mixed(int m, int n, bool gcv) 
     return d + (ints * 4 + 7) / 8;
 }
 // Global scratch of one warp worker (doubles).
-__host__ __device__ inline long warp_scratch_doubles(int m, int n, int K) {
+// Offset of the mixed method's FP32 basis (m x n floats) in it, after the
+// per-voxel basis, surrogate samples, L-curve caches, singular values and the
+// stored solutions.
+__host__ __device__ inline long warp_scratch_f32_offset(int m, int n, int K) {
     int mn = m < n ? m : n;
     return (long)m * n + 3L * K + (long)kCacheCap * (3 + 4 + 12) + mn + 16 + (long)kSolCap * (n + 1);
+}
+__host__ __device__ inline long warp_scratch_doubles(int m, int n, int K) {
+    return warp_scratch_f32_offset(m, n, K) + ((long)m * n + 1) / 2;
 }
 
 }  // namespace dk
