@@ -25,7 +25,7 @@
 #include "decaes_gpu.h"
 #include "epg.cuh"
 #include "host.h"
-#include "t2map_device.cuh"
+#include "voxel_kernels.cuh"
 
 namespace dk {
 
@@ -130,137 +130,11 @@ __global__ void k_compact_range(const void *image, int f32, long v0, long v1, do
     }
 }
 
-// Points one warp's views at its shared-memory workspace p and global scratch
-// scr for the problem shape of P.
-__device__ void warp_setup(Warp &w, const Params &P, double *p, double *scr) {
-    w.P = &P;
-    w.mixed = P.mixed != 0;
-    const int n = P.n, lda = P.lda;
-    if (w.mixed) {
-        // normal-equation workspace (see warp_smem_doubles_mixed)
-        const int m = P.m;
-        w.data = p; p += m;
-        w.s.x = p; p += n;
-        w.s.w = p; p += n;
-        w.xout = p; p += n;
-        w.g.G = p; p += mixed_r1_doubles(m, n);
-        w.g.L = p; p += mixed_r2_doubles(m, n, P.reg == 2);
-        w.g.f = p; p += n;
-        w.g.y = p; p += n;
-        w.g.dd = p; p += n;
-        w.g.dinv = p; p += n;
-        w.g.xp = p; p += n;
-        p += 8;
-        int *ip = reinterpret_cast<int *>(p);
-        w.s.idx = ip;
-        w.g.P = ip + n;
-        w.g.pos = ip + 2 * n;
-        w.g.lastP = ip + 3 * n;
-        w.g.lastk = 0;
-        w.As32 = reinterpret_cast<float *>(w.g.L);  // the staged basis is consumed before the first factorization
-        w.ldA = m | 1;
-        w.s.C = w.g.L;
-        w.s.zz = w.g.y;
-        w.s.b = nullptr; w.s.rdiag = nullptr; w.s.posof = nullptr; w.s.zl = nullptr; w.s.diag = nullptr;
-        w.s.lda = lda;
-    } else {
-        w.s.C = p; p += (long)lda * n;
-        w.s.b = p; p += lda;
-        w.s.zz = p; p += lda;
-        w.data = p; p += lda;
-        w.s.x = p; p += n;
-        w.s.w = p; p += n;
-        w.xout = p; p += n;
-        w.s.rdiag = p; p += n;
-        p += 8;
-        w.s.idx = reinterpret_cast<int *>(p);
-        w.s.posof = w.s.idx + n;
-        w.s.zl = w.s.posof + n;
-        w.s.diag = reinterpret_cast<unsigned char *>(w.s.zl + 2 * n);
-        w.s.lda = lda;
-    }
-    w.scr = scr;
-    const int mn = P.m < P.n ? P.m : P.n;
-    w.sol_key = w.scr + (long)P.m * n + 3L * P.K + (long)kCacheCap * 19 + mn + 16;
-    w.sol_x = w.sol_key + kSolCap;
-    w.nsol = 0;
-}
-
-// Persistent voxel solver: one warp per voxel, voxels pulled from a counter;
-// blockDim.x / 32 warps per block, each with its own workspace.  P.mixed
-// selects the method (warp-uniform for the whole launch).
-__global__ void __launch_bounds__(128) k_voxels(const __grid_constant__ Params P) {
-    extern __shared__ double smem[];
-    const int wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-    Warp w;
-    w.lane = threadIdx.x & 31;
-    w.nnls_caps = 0;
-    w.loop_caps = 0;
-    warp_setup(w, P, smem + (long)wib * P.smem_stride, P.scratch + ((long)blockIdx.x * wpb + wib) * P.scr_stride);
-    const int nvox = *P.nvox;
-    for (;;) {
-        int t = 0;
-        if (w.lane == 0) t = atomicAdd(P.counter, 1);
-        t = __shfl_sync(FULL, t, 0);
-        if (t >= nvox) break;
-        process_voxel(w, (long)P.vidx[t]);
-    }
-    if (w.lane == 0) {
-        if (w.nnls_caps) atomicAdd(&P.stats[0], (unsigned long long)w.nnls_caps);
-        if (w.loop_caps) atomicAdd(&P.stats[1], (unsigned long long)w.loop_caps);
-    }
-}
-
-// Many volumes in one persistent launch (the batched path).  The compacted
-// voxel lists of all volumes form one queue in the order of B.offsets (the
-// host orders volumes by estimated cost, most expensive first, so the tail of
-// the launch is made of cheap voxels).  A warp that moves to another volume
-// copies that volume's parameters next to its workspace and re-carves the
-// workspace for the volume's (nTE, nT2, method).
-__global__ void __launch_bounds__(128) k_voxels_batch(const __grid_constant__ BatchParams B) {
-    extern __shared__ double smem[];
-    const int wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-    double *base = smem + (long)wib * B.smem_stride;
-    Params *Pw = reinterpret_cast<Params *>(base);
-    double *ws = base + kParamsDoubles;
-    double *scr = B.scratch + ((long)blockIdx.x * wpb + wib) * B.scr_stride;
-    Warp w;
-    w.lane = threadIdx.x & 31;
-    w.nnls_caps = 0;
-    w.loop_caps = 0;
-    int cur = -1;
-    const int total = B.offsets[B.nvol];
-    for (;;) {
-        int t = 0;
-        if (w.lane == 0) t = atomicAdd(B.counter, 1);
-        t = __shfl_sync(FULL, t, 0);
-        if (t >= total) break;
-        int lo = 0, hi = B.nvol - 1;  // last volume whose queue segment starts at or before t
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (B.offsets[mid] <= t) lo = mid; else hi = mid - 1;
-        }
-        if (lo != cur) {
-            if (cur >= 0 && w.lane == 0) {
-                if (w.nnls_caps) atomicAdd(&Pw->stats[0], (unsigned long long)w.nnls_caps);
-                if (w.loop_caps) atomicAdd(&Pw->stats[1], (unsigned long long)w.loop_caps);
-            }
-            w.nnls_caps = 0;
-            w.loop_caps = 0;
-            __syncwarp();
-            const double *src = reinterpret_cast<const double *>(B.vols + lo);
-            for (int q = w.lane; q < kParamsDoubles; q += 32) base[q] = src[q];
-            __syncwarp();
-            warp_setup(w, *Pw, ws, scr);
-            cur = lo;
-        }
-        process_voxel(w, (long)Pw->vidx[t - B.offsets[lo]]);
-    }
-    if (cur >= 0 && w.lane == 0) {
-        if (w.nnls_caps) atomicAdd(&Pw->stats[0], (unsigned long long)w.nnls_caps);
-        if (w.loop_caps) atomicAdd(&Pw->stats[1], (unsigned long long)w.loop_caps);
-    }
-}
+__global__ void __launch_bounds__(128) k_voxels(const __grid_constant__ Params P) { voxels_body(P); }
+__global__ void __launch_bounds__(128) k_voxels_batch(const __grid_constant__ BatchParams B) { voxels_batch_body(B); }
+// the same kernels with the legacy algorithms (decaes_legacy.cu)
+__global__ void __launch_bounds__(128) k_voxels_legacy(const __grid_constant__ Params P);
+__global__ void __launch_bounds__(128) k_voxels_batch_legacy(const __grid_constant__ BatchParams B);
 
 // offsets[0] = 0, offsets[v + 1] = offsets[v] + counts[v] (one thread; nvol is small).
 __global__ void k_batch_prefix(const int *counts, int nvol, int *offsets) {
@@ -344,9 +218,9 @@ struct Basis {
 // Autotuning record per problem shape: warps per block of the voxel kernel
 // and the measured cost per voxel.
 struct TuneKey {
-    int m, n, K, reg, mixed, beta180;
+    int m, n, K, reg, mixed, beta180, legacy;
     bool operator<(const TuneKey &o) const {
-        return std::tie(m, n, K, reg, mixed, beta180) < std::tie(o.m, o.n, o.K, o.reg, o.mixed, o.beta180);
+        return std::tie(m, n, K, reg, mixed, beta180, legacy) < std::tie(o.m, o.n, o.K, o.reg, o.mixed, o.beta180, o.legacy);
     }
 };
 struct Tune {
@@ -517,7 +391,7 @@ int make_params(decaes_ctx *ctx, const decaes_t2map_opts &o, const dh::T2partPla
     P = dk::Params{};
     P.m = m; P.n = n; P.K = fixed ? 1 : o.nRefAngles; P.M = m + n; P.lda = (m + n) | 1;
     P.reg = o.Reg; P.chi2factor = o.Chi2Factor; P.noiselevel = o.NoiseLevel;
-    P.mineval = o.nRefAnglesMin; P.maxeval = o.nRefAngles;
+    P.mineval = o.nRefAnglesMin; P.maxeval = o.nRefAngles; P.legacy = o.legacy ? 1 : 0;
     P.angle_mode = d_b1 ? 2 : (fixed ? 1 : 0);
     P.fixed_angle = o.SetFlipAngle;
     P.beta180 = o.RefConAngle == 180.0; P.beta = o.RefConAngle; P.TE = o.TE; P.T1 = o.T1;
@@ -553,7 +427,8 @@ int make_params(decaes_ctx *ctx, const decaes_t2map_opts &o, const dh::T2partPla
 int tuned_wpb(decaes_ctx *ctx, const decaes_t2map_opts &o) {
     if (ctx->force_wpb) return ctx->force_wpb;
     const bool fixed = !std::isnan(o.SetFlipAngle);
-    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, o.precision == DECAES_PREC_MIXED, o.RefConAngle == 180.0};
+    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, o.precision == DECAES_PREC_MIXED, o.RefConAngle == 180.0,
+              o.legacy != 0};
     auto it = ctx->tune.find(k);
     return it == ctx->tune.end() ? 1 : it->second.wpb;
 }
@@ -623,12 +498,13 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
     P.smem_stride = wsm;
     int wpb = tuned_wpb(ctx, o), grid = 0;
     size_t smem = 0;
-    if (int rc = launch_shape(ctx, dk::k_voxels, wsm, &wpb, &grid, &smem)) return rc;
+    auto kern = o.legacy ? dk::k_voxels_legacy : dk::k_voxels;
+    if (int rc = launch_shape(ctx, kern, wsm, &wpb, &grid, &smem)) return rc;
     void *scr;
     if (int rc = buf(ctx, "scratch", sizeof(double) * (size_t)P.scr_stride * grid * wpb, &scr)) return rc;
     P.scratch = (double *)scr;
     cudaEventRecord(ctx->ev[2], st);
-    dk::k_voxels<<<grid, 32 * wpb, smem, st>>>(P);
+    kern<<<grid, 32 * wpb, smem, st>>>(P);
     cudaEventRecord(ctx->ev[3], st);
     ++nl;
     CK(cudaGetLastError());
@@ -691,11 +567,11 @@ int check_both(decaes_ctx *ctx, const decaes_t2map_opts *mo, const decaes_t2part
     if (dtype != DECAES_F32 && dtype != DECAES_F64) return fail(ctx, DECAES_EINVAL, "dtype must be DECAES_F32 or DECAES_F64");
     if (mo) {
         std::string e = dh::check_t2map(*mo);
-        if (!e.empty()) return fail(ctx, mo->legacy ? DECAES_ELEGACY : DECAES_EINVAL, e);
+        if (!e.empty()) return fail(ctx, DECAES_EINVAL, e);
     }
     if (po) {
         std::string e = dh::check_t2part(*po);
-        if (!e.empty()) return fail(ctx, po->legacy ? DECAES_ELEGACY : DECAES_EINVAL, e);
+        if (!e.empty()) return fail(ctx, DECAES_EINVAL, e);
         if (mo) {
             if (po->nT2 != mo->nT2) return fail(ctx, DECAES_EINVAL, "T2part nT2 must equal T2map nT2");
             for (int d = 0; d < 3; ++d)
@@ -1003,6 +879,7 @@ struct BatchPrep {
     long smem_stride = 0, scr_stride = 0;
     int wpb = 1, grid = 0;
     size_t smem = 0;
+    bool legacy = false;  // some volume uses the legacy algorithms: the legacy kernel runs the batch
     size_t cnt_bytes() const { return sizeof(int) * (2 * vols.size() + 2) + 16; }
 };
 
@@ -1010,12 +887,13 @@ struct BatchPrep {
 // methods' measured costs (FP64 GCV ~35x the mixed method, FP64 ~5x mixed).
 double voxel_cost(decaes_ctx *ctx, const decaes_t2map_opts &o) {
     const bool fixed = !std::isnan(o.SetFlipAngle), mixed = o.precision == DECAES_PREC_MIXED;
-    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, mixed, o.RefConAngle == 180.0};
+    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, mixed, o.RefConAngle == 180.0, o.legacy != 0};
     auto it = ctx->tune.find(k);
     if (it != ctx->tune.end() && it->second.us_per_voxel > 0) return it->second.us_per_voxel;
     double c = 1e-4 * o.nTE * o.nT2;
     if (o.Reg == DECAES_REG_LCURVE || o.Reg == DECAES_REG_GCV) c *= 3;
     if (!mixed) c *= (o.Reg == DECAES_REG_GCV) ? 35 : 5;
+    if (o.legacy && !fixed) c += 0.002 * (180.0 - o.MinRefAngle);  // the sampled spline minimum (~30 us per voxel over 50-180)
     return c;
 }
 
@@ -1067,8 +945,11 @@ int batch_plan(decaes_ctx *ctx, const decaes_volume *vols, int nvol, cudaStream_
         bp.scr_stride = std::max(bp.scr_stride, P.scr_stride);
     }
     bp.smem_stride = (bp.smem_stride + 1) & ~1L;
+    bp.legacy = false;
+    for (const BatchVol &bv : bp.vols) bp.legacy = bp.legacy || bv.v.mopts.legacy;
     bp.wpb = tuned_wpb(ctx, bp.vols[0].v.mopts);
-    return launch_shape(ctx, dk::k_voxels_batch, bp.smem_stride, &bp.wpb, &bp.grid, &bp.smem);
+    return launch_shape(ctx, bp.legacy ? dk::k_voxels_batch_legacy : dk::k_voxels_batch, bp.smem_stride, &bp.wpb,
+                        &bp.grid, &bp.smem);
 }
 
 size_t batch_bytes(const BatchPrep &bp, size_t *b_out, size_t *b_vidx, size_t *b_w, size_t *b_par, size_t *b_scr) {
@@ -1128,7 +1009,7 @@ int batch_enqueue(decaes_ctx *ctx, const BatchPrep &bp, cudaStream_t st, int *la
     }
     dk::k_batch_prefix<<<1, 32, 0, st>>>(counts, nvol, offsets);
     dk::BatchParams B{bp.params, offsets, nvol, counter, bp.scratch, bp.scr_stride, bp.smem_stride};
-    dk::k_voxels_batch<<<bp.grid, 32 * bp.wpb, bp.smem, st>>>(B);
+    (bp.legacy ? dk::k_voxels_batch_legacy : dk::k_voxels_batch)<<<bp.grid, 32 * bp.wpb, bp.smem, st>>>(B);
     *launches += 2;
     for (int q = 0; q < nvol; ++q) {
         const BatchVol &bv = bp.vols[q];
@@ -1331,7 +1212,8 @@ extern "C" int decaes_autotune(decaes_ctx *ctx, const decaes_t2map_opts *opts, d
     }
     ctx->force_wpb = 0;
     const bool fixed = !std::isnan(o.SetFlipAngle);
-    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, o.precision == DECAES_PREC_MIXED, o.RefConAngle == 180.0};
+    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, o.precision == DECAES_PREC_MIXED, o.RefConAngle == 180.0,
+              o.legacy != 0};
     Tune t;
     t.wpb = best_w;
     t.us_per_voxel = best_ms * 1e3 / (double)V;
@@ -1583,9 +1465,12 @@ std::vector<Chunk> srv_launch_tick(decaes_server *S) {
     smem_stride = (smem_stride + 1) & ~1L;
     int wpb = 1, grid = 0;
     size_t smem = 0;
+    bool legacy = false;
+    for (int q = 0; q < nq; ++q) legacy = legacy || ch[q].r->mo.legacy;
+    auto kern = legacy ? dk::k_voxels_batch_legacy : dk::k_voxels_batch;
     if (ok) {
         wpb = tuned_wpb(ctx, ch[0].r->mo);
-        ok = launch_shape(ctx, dk::k_voxels_batch, smem_stride, &wpb, &grid, &smem) == DECAES_OK;
+        ok = launch_shape(ctx, kern, smem_stride, &wpb, &grid, &smem) == DECAES_OK;
     }
     const size_t need = sizeof(double) * (size_t)scr_stride * grid * wpb;
     if (ok && need > S->scratch_bytes) {
@@ -1612,7 +1497,7 @@ std::vector<Chunk> srv_launch_tick(decaes_server *S) {
         }
         dk::k_batch_prefix<<<1, 32, 0, st>>>(counts, nq, offsets);
         dk::BatchParams B{S->d_params, offsets, nq, counter, S->d_scratch, scr_stride, smem_stride};
-        dk::k_voxels_batch<<<grid, 32 * wpb, smem, st>>>(B);
+        kern<<<grid, 32 * wpb, smem, st>>>(B);
         ok = cudaGetLastError() == cudaSuccess && cudaEventRecord(S->tick_t1, st) == cudaSuccess;
     }
     if (!ok) {

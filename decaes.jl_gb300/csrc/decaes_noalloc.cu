@@ -38,6 +38,7 @@ __global__ void k_basis_fixed(int m, int n, double alpha, double TE, double T1, 
 __global__ void k_fill(double *p, long len, double v);
 __global__ void k_compact(const void *image, int f32, long V, double thr, int *vidx, int *nvox);
 __global__ void __launch_bounds__(128) k_voxels(const __grid_constant__ Params P);
+__global__ void __launch_bounds__(128) k_voxels_legacy(const __grid_constant__ Params P);
 }  // namespace dk
 
 namespace {
@@ -120,12 +121,12 @@ extern "C" int decaes_t2map_t2part_noalloc(const decaes_t2map_opts *mopts, const
     const decaes_t2map_opts &o = *mopts;
     {
         std::string e = dh::check_t2map(o);
-        if (!e.empty()) return fail(err, errlen, o.legacy ? DECAES_ELEGACY : DECAES_EINVAL, e);
+        if (!e.empty()) return fail(err, errlen, DECAES_EINVAL, e);
     }
     dh::T2partPlan pp{};
     if (popts) {
         std::string e = dh::check_t2part(*popts);
-        if (!e.empty()) return fail(err, errlen, popts->legacy ? DECAES_ELEGACY : DECAES_EINVAL, e);
+        if (!e.empty()) return fail(err, errlen, DECAES_EINVAL, e);
         if (popts->nT2 != o.nT2) return fail(err, errlen, DECAES_EINVAL, "T2part nT2 must equal T2map nT2");
         for (int d = 0; d < 3; ++d)
             if (popts->MatrixSize[d] != o.MatrixSize[d])
@@ -183,9 +184,10 @@ extern "C" int decaes_t2map_t2part_noalloc(const decaes_t2map_opts *mopts, const
                     "problem needs " + std::to_string(need_min) + " bytes of the " + std::to_string(kStaticBytes) +
                         "-byte static workspace (grows with the voxel count, nTE*nT2*nRefAngles and nT2); "
                         "split the image into smaller slabs");
-    NA_CK(cudaFuncSetAttribute(dk::k_voxels, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    auto kern = o.legacy ? dk::k_voxels_legacy : dk::k_voxels;
+    NA_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    NA_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dk::k_voxels, 32, smem));
+    NA_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem));
     if (per_sm < 1) return fail(err, errlen, DECAES_EINVAL, "voxel kernel cannot be resident with this workspace size");
     const long fit = (long)((kStaticBytes - o_scr) / warp_bytes);
     const int grid = (int)std::max<long>(1, std::min<long>((long)per_sm * ds.sms, fit));
@@ -246,7 +248,7 @@ extern "C" int decaes_t2map_t2part_noalloc(const decaes_t2map_opts *mopts, const
 
     // Persistent voxel solve.
     P.reg = o.Reg; P.chi2factor = o.Chi2Factor; P.noiselevel = o.NoiseLevel;
-    P.mineval = o.nRefAnglesMin; P.maxeval = o.nRefAngles;
+    P.mineval = o.nRefAnglesMin; P.maxeval = o.nRefAngles; P.legacy = o.legacy ? 1 : 0;
     P.angle_mode = d_b1map ? 2 : (fixed ? 1 : 0);
     P.fixed_angle = o.SetFlipAngle;
     P.beta180 = beta180; P.beta = o.RefConAngle; P.TE = o.TE; P.T1 = o.T1;
@@ -267,7 +269,7 @@ extern "C" int decaes_t2map_t2part_noalloc(const decaes_t2map_opts *mopts, const
     }
     P.epg_lanes = (int)std::min<long>(32, ((long)P.lda * n) / (3L * m));
     P.scratch = dptr(o_scr);
-    dk::k_voxels<<<grid, 32, smem, st>>>(P);
+    kern<<<grid, 32, smem, st>>>(P);
     NA_CK(cudaGetLastError());
     return DECAES_OK;
 }

@@ -186,7 +186,6 @@ static std::string nothing_or(double v) { return std::isnan(v) ? "nothing" : jlf
 
 std::string check_t2map(const decaes_t2map_opts &o) {
     char b[512];
-    if (o.legacy) return "legacy = true: the legacy algorithms are not provided by this library.";
     if (o.MatrixSize[0] < 1 || o.MatrixSize[1] < 1 || o.MatrixSize[2] < 1) {
         std::snprintf(b, sizeof b, "MatrixSize must be a tuple of 3 positive integers, but MatrixSize = (%d, %d, %d).",
                       o.MatrixSize[0], o.MatrixSize[1], o.MatrixSize[2]);
@@ -224,7 +223,6 @@ std::string check_t2map(const decaes_t2map_opts &o) {
 }
 
 std::string check_t2part(const decaes_t2part_opts &o) {
-    if (o.legacy) return "legacy = true: the legacy algorithms are not provided by this library.";
     if (o.MatrixSize[0] < 1 || o.MatrixSize[1] < 1 || o.MatrixSize[2] < 1) return "all(MatrixSize .>= 1)";
     if (!(o.nT2 >= 2)) return "nT2 >= 2";
     if (!(0.0 < o.T2Range[0] && o.T2Range[0] < o.T2Range[1])) return "0.0 < T2Range[1] < T2Range[2]";
@@ -345,11 +343,11 @@ extern "C" int decaes_mock_image(const decaes_mock_opts *opts, uint64_t seed, vo
 extern "C" int decaes_t2map_check_options(const decaes_t2map_opts *opts, char *msg, size_t msglen) {
     std::string e = opts ? dh::check_t2map(*opts) : std::string("opts is NULL");
     if (msg && msglen) { std::strncpy(msg, e.c_str(), msglen - 1); msg[msglen - 1] = 0; }
-    return e.empty() ? DECAES_OK : (opts && opts->legacy ? DECAES_ELEGACY : DECAES_EINVAL);
+    return e.empty() ? DECAES_OK : DECAES_EINVAL;
 }
 
 extern "C" int decaes_t2part_check_options(const decaes_t2part_opts *opts, char *msg, size_t msglen) {
     std::string e = opts ? dh::check_t2part(*opts) : std::string("opts is NULL");
     if (msg && msglen) { std::strncpy(msg, e.c_str(), msglen - 1); msg[msglen - 1] = 0; }
-    return e.empty() ? DECAES_OK : (opts && opts->legacy ? DECAES_ELEGACY : DECAES_EINVAL);
+    return e.empty() ? DECAES_OK : DECAES_EINVAL;
 }

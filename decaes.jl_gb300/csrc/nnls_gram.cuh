@@ -103,7 +103,7 @@ __device__ __forceinline__ double widen(float f) {
 }
 
 // b'b.
-__device__ void gram_bb(GramWS &g, int m, const double *b) {
+static __device__ void gram_bb(GramWS &g, int m, const double *b) {
     const int lane = threadIdx.x & 31;
     double part = 0.0;
     #pragma unroll 1
@@ -113,7 +113,7 @@ __device__ void gram_bb(GramWS &g, int m, const double *b) {
 
 // f = A'b from a row-major (transposed, m x n) basis in global memory: lanes
 // over columns, coalesced over each row.
-__device__ __noinline__ void gram_rhs_t(GramWS &g, const double *AT, int m, int n, const double *b) {
+static __device__ __noinline__ void gram_rhs_t(GramWS &g, const double *AT, int m, int n, const double *b) {
     const int lane = threadIdx.x & 31;
     #pragma unroll 1
     for (int j = lane; j < n; j += 32) {
@@ -136,7 +136,7 @@ __device__ __noinline__ void gram_rhs_t(GramWS &g, const double *AT, int m, int 
 // EPG curves themselves, so the products are exact in FP64 and G is the Gram
 // matrix of the basis to FP64 rounding.  Lanes over columns for f and over the
 // n(n+1)/2 upper-triangle entries for G.
-__device__ __noinline__ void gram_build_f32(GramWS &g, const float *As, int lda, int m, int n, const double *b) {
+static __device__ __noinline__ void gram_build_f32(GramWS &g, const float *As, int lda, int m, int n, const double *b) {
     const int lane = threadIdx.x & 31;
     #pragma unroll 1
     for (int j = lane; j < n; j += 32) {
@@ -174,7 +174,7 @@ __device__ __noinline__ void gram_build_f32(GramWS &g, const float *As, int lda,
 }
 
 // G copied from a precomputed packed Gram matrix in global memory.
-__device__ __noinline__ void gram_load(GramWS &g, const double *Gg, int n) {
+static __device__ __noinline__ void gram_load(GramWS &g, const double *Gg, int n) {
     const int lane = threadIdx.x & 31;
     const int np = tri(n);
 #pragma unroll 4
@@ -188,7 +188,7 @@ __device__ __noinline__ void gram_load(GramWS &g, const double *Gg, int n) {
 // update spread over lanes by (row, column) pair, so a step costs ~(k-j)^2/64
 // FMA instructions instead of k-j.  Returns false when a pivot is not
 // positive relative to its diagonal (numerically dependent set).
-__device__ bool gram_refactor(GramWS &g, int k, double mu2) {
+static __device__ bool gram_refactor(GramWS &g, int k, double mu2) {
     const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;
     const int p0 = r0 < k ? g.P[r0] : 0, p1 = r1 < k ? g.P[r1] : 0;
@@ -255,7 +255,7 @@ __device__ bool gram_refactor(GramWS &g, int k, double mu2) {
 // not positive relative to H_tt or when its coefficient y_t / delta in the
 // unconstrained solution on P + {t} is not positive (the guards of the
 // reference's Householder step).  Returns true when t was added.
-__device__ bool gram_append(GramWS &g, int k, int t, double mu2) {
+static __device__ bool gram_append(GramWS &g, int k, int t, double mu2) {
     const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;
     const double *L0 = g.L + tri(r0 - 1), *L1 = g.L + tri(r1 - 1);
@@ -291,7 +291,7 @@ __device__ bool gram_append(GramWS &g, int k, int t, double mu2) {
 
 // z = L^{-T} D^{-1} y (unit upper back substitution, lanes over rows);
 // z returned in (z0, z1).
-__device__ void gram_back(const GramWS &g, int k, double &z0, double &z1) {
+static __device__ void gram_back(const GramWS &g, int k, double &z0, double &z1) {
     const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;
     double u0 = r0 < k ? g.y[r0] * g.dinv[r0] : 0.0, u1 = r1 < k ? g.y[r1] * g.dinv[r1] : 0.0;
@@ -321,7 +321,7 @@ __device__ void gram_back(const GramWS &g, int k, double &z0, double &z1) {
 // absolute 1e-15 * bound.  Writes the min(m,n) largest square roots in
 // descending order to gam (zeros for the unresolved ones).  Uses y, xp, dd and
 // dinv as scratch (free before the first solve) and W (tri(n) doubles).
-__device__ __noinline__ void gram_svdvals(GramWS g, double *W, int m, int n, double *gam) {
+static __device__ __noinline__ void gram_svdvals(GramWS g, double *W, int m, int n, double *gam) {
     const int lane = threadIdx.x & 31;
     const int np = tri(n);
 #pragma unroll 1
@@ -456,7 +456,7 @@ __device__ __noinline__ void gram_svdvals(GramWS g, double *W, int m, int n, dou
 // holds the solution, idx its passive columns (1-based, nsetp entries) and
 // rnorm^2 = ||A x - b||^2 + mu2 ||x||^2.  mode = 1 when max_iter was reached
 // (the reference's cap 3n).
-__device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double *wv, int *idx, int n, double mu2,
+static __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double *wv, int *idx, int n, double mu2,
                                              int max_iter, int *lastk_io) {
     const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;

@@ -109,7 +109,7 @@ __device__ __forceinline__ double &Aat(const NnlsWS &s, int i1, int j1) {
 
 // Base.hypot for Float64 (C. F. Borges, "An Improved Algorithm for
 // hypot(a,b)", 2019, fma-corrected), used by NNLS.orthogonal_rotmat.
-__device__ double jl_hypot(double x, double y) {
+static __device__ double jl_hypot(double x, double y) {
     if (isinf(x) || isinf(y)) return CUDART_INF;
     double ax = fabs(x), ay = fabs(y);
     if (ay > ax) { double t = ax; ax = ay; ay = t; }
@@ -130,7 +130,7 @@ __device__ double jl_hypot(double x, double y) {
 
 // construct_apply_householder!(A, b, ip, jp, m), src/NNLS.jl:259-336.
 // Writes only the pivot column's physical storage (see header note).
-__device__ double warp_cah(const NnlsWS &s, int ip, int jp, int m) {
+static __device__ double warp_cah(const NnlsWS &s, int ip, int jp, int m) {
     const int lane = threadIdx.x & 31;
     if (ip > m) return 0.0;
     double *col = s.C + (size_t)(s.idx[jp - 1] - 1) * s.lda;  // pivot column (0-based rows)
@@ -187,7 +187,7 @@ __device__ double warp_cah(const NnlsWS &s, int ip, int jp, int m) {
 
 // apply_householder_dual!(A, w, b, tau, j1, m1), src/NNLS.jl:379-436.
 // Lanes over logical columns j1+1..n.
-__device__ void warp_ahd(const NnlsWS &s, int n, double tau, int j1, int m1) {
+static __device__ void warp_ahd(const NnlsWS &s, int n, double tau, int j1, int m1) {
     const int lane = threadIdx.x & 31;
     if (j1 >= m1) return;
     const double *u = s.C + (size_t)(s.idx[j1 - 1] - 1) * s.lda;  // u[j1-1] is the diagonal; treated as 1
@@ -214,7 +214,7 @@ __device__ void warp_ahd(const NnlsWS &s, int n, double tau, int j1, int m1) {
 }
 
 // compute_dual!(w, A, b, j1, m1), src/NNLS.jl:441-470.  Lanes over columns.
-__device__ void warp_compute_dual(const NnlsWS &s, int n, int j1, int m1) {
+static __device__ void warp_compute_dual(const NnlsWS &s, int n, int j1, int m1) {
     const int lane = threadIdx.x & 31;
     const int nz = warp_active_cols(s, n, j1);
     for (int r0 = 0; r0 < nz; r0 += 32) {
@@ -232,7 +232,7 @@ __device__ void warp_compute_dual(const NnlsWS &s, int n, int j1, int m1) {
 
 // zz[1:n] = b[1:n]; solve_triangular_system!(zz, A, n), src/NNLS.jl:506-523.
 // Lanes over rows; the column sweep is sequential as in the reference.
-__device__ void warp_solve_tri(const NnlsWS &s, int n) {
+static __device__ void warp_solve_tri(const NnlsWS &s, int n) {
     const int lane = threadIdx.x & 31;
     for (int i = lane; i < n; i += 32) s.zz[i] = s.b[i];
     __syncwarp();
@@ -248,7 +248,7 @@ __device__ void warp_solve_tri(const NnlsWS &s, int n) {
 }
 
 // Transposed solve (U' z = x) on the first n logical columns, src/NNLS.jl:524-537.
-__device__ void warp_solve_tri_t(const NnlsWS &s, double *z, int n) {
+static __device__ void warp_solve_tri_t(const NnlsWS &s, double *z, int n) {
     const int lane = threadIdx.x & 31;
     for (int j = 1; j <= n; ++j) {
         const double *a = s.C + (size_t)(s.idx[j - 1] - 1) * s.lda;
@@ -291,7 +291,7 @@ struct NnlsResult {
 
 // Main + secondary loops of unsafe_nnls! (tikh = false) and of its Tikhonov
 // form (tikh = true, rows M = m0 + n with lazily activated padding rows).
-__device__ NnlsResult warp_nnls(const NnlsWS &s, int M, int n, int m0, bool tikh, double lam, int max_iter) {
+static __device__ NnlsResult warp_nnls(const NnlsWS &s, int M, int n, int m0, bool tikh, double lam, int max_iter) {
     const int lane = threadIdx.x & 31;
     int m = tikh ? m0 : M;
     int nsetp = 0, iter = 0, mode = 0;
@@ -461,7 +461,7 @@ __device__ NnlsResult warp_nnls(const NnlsWS &s, int M, int n, int m0, bool tikh
 // `data` is the (shared-memory) right-hand side; it is not modified.
 // Not inlined: every caller shares one copy of the NNLS code (instruction
 // cache), and the workspace views travel in registers.
-__device__ __noinline__ NnlsResult warp_lsq(const NnlsWS s, const double *A, int m, int n, const double *data,
+static __device__ __noinline__ NnlsResult warp_lsq(const NnlsWS s, const double *A, int m, int n, const double *data,
                                             bool tikh, double mu) {
     const int lane = threadIdx.x & 31;
     const int M = tikh ? m + n : m;
@@ -508,7 +508,7 @@ __device__ __noinline__ NnlsResult warp_lsq(const NnlsWS s, const double *A, int
 }
 
 // sum(abs2, positive_solution): ||x||^2 over the active set in set-P order.
-__device__ double warp_seminorm_sq(const NnlsWS &s, int nsetp) {
+static __device__ double warp_seminorm_sq(const NnlsWS &s, int nsetp) {
     const int lane = threadIdx.x & 31;
     double part = 0.0;
     for (int i = lane; i < nsetp; i += 32) {

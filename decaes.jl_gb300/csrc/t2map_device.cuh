@@ -5,10 +5,20 @@
 #pragma once
 #include "epg.cuh"
 #include "nnls_gram.cuh"
+#include "legacy.cuh"
 #include "nnls_warp.cuh"
 #include "t2map_params.cuh"
 
+// The legacy algorithms are compiled only into the kernels of the translation
+// unit that defines DECAES_LEGACY_KERNEL=1; elsewhere kLegacyKernel is false
+// and the legacy branches fold away.
+#ifndef DECAES_LEGACY_KERNEL
+#define DECAES_LEGACY_KERNEL 0
+#endif
+
 namespace dk {
+
+constexpr bool kLegacyKernel = DECAES_LEGACY_KERNEL != 0;
 
 struct Warp {
     const Params *P;
@@ -33,7 +43,7 @@ __device__ __forceinline__ void note(Warp &w, const NnlsResult &r) { w.nnls_caps
 // Unregularized (tikh = false) or Tikhonov solve on the voxel's basis w.A:
 // the reference's Householder NNLS for the plain method, the normal-equation
 // solver on the voxel's prepared Gram matrix for the mixed method.
-__device__ NnlsResult basis_lsq(Warp &w, bool tikh, double mu) {
+static __device__ NnlsResult basis_lsq(Warp &w, bool tikh, double mu) {
     const Params &P = *w.P;
     if (w.mixed)
         return gram_nnls(w.g, w.s.x, w.s.w, w.s.idx, P.n, tikh ? mu * mu : 0.0, 3 * P.n, &w.g.lastk);
@@ -53,7 +63,7 @@ __device__ __forceinline__ bool isapprox(double x, double y) {
     return fabs(x - y) <= jmax(0.0, 1.4901161193847656e-08 * jmax(fabs(x), fabs(y)));
 }
 // First i in [0, len) with isapprox(x, keys[i]), or -1; lanes over entries.
-__device__ int warp_find_approx(const double *keys, int len, double x) {
+static __device__ int warp_find_approx(const double *keys, int len, double x) {
     const int lane = threadIdx.x & 31;
     #pragma unroll 1
     for (int c = 0; c < len; c += 32) {
@@ -65,7 +75,7 @@ __device__ int warp_find_approx(const double *keys, int len, double x) {
     return -1;
 }
 // First i with keys[i] == x exactly (as doubles), or -1.
-__device__ int warp_find_exact(const double *keys, int len, double x) {
+static __device__ int warp_find_exact(const double *keys, int len, double x) {
     const int lane = threadIdx.x & 31;
     #pragma unroll 1
     for (int c = 0; c < len; c += 32) {
@@ -77,7 +87,7 @@ __device__ int warp_find_exact(const double *keys, int len, double x) {
     return -1;
 }
 // Store the current Tikhonov solution s.x under key log mu.
-__device__ void sol_store(Warp &w, double logmu) {
+static __device__ void sol_store(Warp &w, double logmu) {
     if (w.nsol >= kSolCap) return;
     const int n = w.P->n;
     double *dst = w.sol_x + (long)w.nsol * n;
@@ -89,7 +99,7 @@ __device__ void sol_store(Warp &w, double logmu) {
 }
 // The solution at mu = exp(logmu): from the store when this exact key was
 // solved before (the solve is deterministic), else solved now.  Result in xout.
-__device__ void final_solution(Warp &w, double logmu);
+static __device__ void final_solution(Warp &w, double logmu);
 
 // ----------------------------------------------------------------------------
 // Tikhonov helpers (src/lsqnonneg.jl:297-318)
@@ -98,24 +108,24 @@ struct TikhState {
     NnlsResult r;
     double mu;
 };
-__device__ TikhState tikh_solve(Warp &w, double mu) {
+static __device__ TikhState tikh_solve(Warp &w, double mu) {
     TikhState t;
     t.r = basis_lsq(w, true, mu);
     t.mu = mu;
     note(w, t.r);
     return t;
 }
-__device__ double tikh_res2(Warp &w, const TikhState &t) {
+static __device__ double tikh_res2(Warp &w, const TikhState &t) {
     double ssq = warp_seminorm_sq(w.s, t.r.nsetp);
     return jmax(__dsub_rn(__dmul_rn(t.r.rnorm, t.r.rnorm), __dmul_rn(__dmul_rn(t.mu, t.mu), ssq)), 0.0);
 }
-__device__ void save_x(Warp &w) {
+static __device__ void save_x(Warp &w) {
     #pragma unroll 1
     for (int j = w.lane; j < w.P->n; j += 32) w.xout[j] = w.s.x[j];
     __syncwarp();
 }
 
-__device__ void final_solution(Warp &w, double logmu) {
+static __device__ void final_solution(Warp &w, double logmu) {
     int i = warp_find_exact(w.sol_key, w.nsol, logmu);
     if (i >= 0) {
         const double *src = w.sol_x + (long)i * w.P->n;
@@ -135,7 +145,7 @@ __device__ __forceinline__ double jsign(double x) { return x < 0 ? -1.0 : (x > 0
 
 // bracket_root_monotonic, src/optimization.jl:191-219
 template <class F>
-__device__ void bracket_root_monotonic(F &f, double a, double delta, double dilate, double mono, int maxiters, double &ra,
+static __device__ void bracket_root_monotonic(F &f, double a, double delta, double dilate, double mono, int maxiters, double &ra,
                                        double &rb, double &rfa, double &rfb) {
     double fa = f(a);
     if (!isfinite(fa)) { ra = rb = a; rfa = rfb = CUDART_NAN; return; }
@@ -162,7 +172,7 @@ __device__ void bracket_root_monotonic(F &f, double a, double delta, double dila
 
 // brent_root, src/optimization.jl:71-128
 template <class F>
-__device__ void brent_root(F &f, double x0, double x1, double fx0, double fx1, double xatol, double xrtol, double ftol,
+static __device__ void brent_root(F &f, double x0, double x1, double fx0, double fx1, double xatol, double xrtol, double ftol,
                            int maxiters, double &xr, double &fxr) {
     if (fx0 == 0) { xr = x0; fxr = fx0; return; }
     if (fx1 == 0) { xr = x1; fxr = fx1; return; }
@@ -203,7 +213,7 @@ __device__ void brent_root(F &f, double x0, double x1, double fx0, double fx1, d
 
 // brent_minimize, src/optimization.jl:319-413
 template <class F>
-__device__ void brent_minimize(F &f, double x1, double x2, double xrtol, double xatol, int maxiters, double &xo, double &yo) {
+static __device__ void brent_minimize(F &f, double x1, double x2, double xrtol, double xatol, int maxiters, double &xo, double &yo) {
     const double PHI = 1.6180339887498949;
     const double alpha = 2 - PHI;
     double x = x1 + alpha * (x2 - x1);
@@ -277,7 +287,7 @@ struct MdpF {  // f(logμ) of lsqnonneg_mdp!, src/lsqnonneg.jl:723-726
 // lsqnonneg_chi2! (method :brent), src/lsqnonneg.jl:504-593.  The solution
 // that save_results! stores ends up in w.xout.  On the early exit the
 // reference saves its smoothing cache's stale slot; x_unreg is stored here.
-__device__ void reg_chi2(Warp &w, double chi2_target, double &mu_out, double &chi2_out) {
+static __device__ void reg_chi2(Warp &w, double chi2_target, double &mu_out, double &chi2_out) {
     const Params &P = *w.P;
     NnlsResult r0 = basis_lsq(w, false, 0.0);
     note(w, r0);
@@ -311,9 +321,58 @@ __device__ void reg_chi2(Warp &w, double chi2_target, double &mu_out, double &ch
     chi2_out = res2 / res2_min;
 }
 
+// The legacy algorithms' workspace: the L-curve cache region of the warp's
+// global scratch (the L-curve is not run in the same voxel step).
+static_assert(legacy_ws_doubles(kLegacyMaxPts) + 3 <= (long)kCacheCap * 19 &&
+                  legacy_ws_doubles(kChi2LegacyMaxDouble + 2) + 2 * (kChi2LegacyMaxDouble + 2) <= (long)kCacheCap * 19,
+              "legacy workspace exceeds the L-curve cache region");
+__device__ __forceinline__ double *legacy_ws(Warp &w) { return w.scr + (long)w.P->m * w.P->n + 3L * w.P->K; }
+
+// lsqnonneg_chi2!(legacy = true), src/lsqnonneg.jl:504-531, with
+// chi2_search_from_minimum(legacy = true), src/lsqnonneg.jl:595-636: mu doubles
+// from 1e-3 until res2(mu) >= Chi2Factor * res2_min, then the legacy spline
+// root through every (mu, res2) pair including (0, res2_min); the saved
+// solution is x_unreg when that root is mu = 0.  The doubling stops after
+// kChi2LegacyMaxDouble steps (counted as a loop cap), where the reference
+// would keep doubling on data that never reaches the target.
+static __device__ __noinline__ void reg_chi2_legacy(Warp &w, double chi2_target, double &mu_out, double &chi2_out) {
+    NnlsResult r0 = basis_lsq(w, false, 0.0);
+    note(w, r0);
+    double res2_min = __dmul_rn(r0.rnorm, r0.rnorm);
+    save_x(w);  // x_unreg
+    if (res2_min == 0 || r0.nsetp == 0) { mu_out = 0; chi2_out = 1; return; }
+    double *mus = legacy_ws(w) + legacy_ws_doubles(kChi2LegacyMaxDouble + 2), *r2s = mus + kChi2LegacyMaxDouble + 2;
+    const double target = chi2_target * res2_min;
+    if (w.lane == 0) { mus[0] = 0; r2s[0] = res2_min; }
+    int cnt = 1;
+    double munew = 1e-3;
+    #pragma unroll 1
+    for (int it = 0;; ++it) {
+        TikhState t = tikh_solve(w, munew);
+        double res2new = tikh_res2(w, t);
+        if (w.lane == 0) { mus[cnt] = munew; r2s[cnt] = res2new; }
+        cnt++;
+        if (res2new >= target) break;
+        if (it == kChi2LegacyMaxDouble) { w.loop_caps++; break; }
+        munew *= 2.0;
+    }
+    __syncwarp();
+    const double mu = legacy_scan(mus, r2s, nullptr, cnt, true, target, legacy_ws(w)).x;
+    double res2;
+    if (mu == 0) {
+        res2 = res2_min;
+    } else {
+        TikhState t = tikh_solve(w, mu);
+        res2 = tikh_res2(w, t);
+        save_x(w);
+    }
+    mu_out = mu;
+    chi2_out = res2 / res2_min;
+}
+
 // lsqnonneg_mdp!, src/lsqnonneg.jl:700-747.  Early exits store the returned
 // x (x_unreg or zeros) where the reference saves a stale cache slot.
-__device__ void reg_mdp(Warp &w, double delta, double &mu_out, double &chi2_out) {
+static __device__ void reg_mdp(Warp &w, double delta, double &mu_out, double &chi2_out) {
     const Params &P = *w.P;
     NnlsResult r0 = basis_lsq(w, false, 0.0);
     note(w, r0);
@@ -364,7 +423,7 @@ struct LCurve {
     bool overflow;
 };
 // f_lcurve(logμ) = (log ||Ax-b||^2, log ||x||^2) through the isapprox-keyed cache
-__device__ void lc_eval(LCurve &L, double x, double &P0, double &P1) {
+static __device__ void lc_eval(LCurve &L, double x, double &P0, double &P1) {
     int hit = warp_find_approx(L.fx, L.flen, x);
     if (hit >= 0) { P0 = L.fP[2 * hit]; P1 = L.fP[2 * hit + 1]; return; }
     Warp &w = *L.w;
@@ -382,8 +441,8 @@ __device__ void lc_eval(LCurve &L, double x, double &P0, double &P1) {
         L.overflow = true;
     }
 }
-__device__ int pc_find(const LCurve &L, double x) { return warp_find_approx(L.px, L.plen, x); }
-__device__ void pc_set(LCurve &L, double x, double P0, double P1, double C, bool push_only) {
+static __device__ int pc_find(const LCurve &L, double x) { return warp_find_approx(L.px, L.plen, x); }
+static __device__ void pc_set(LCurve &L, double x, double P0, double P1, double C, bool push_only) {
     int i = push_only ? -1 : pc_find(L, x);
     if (i < 0) {
         if (L.plen >= kCacheCap) { L.overflow = true; return; }
@@ -394,7 +453,7 @@ __device__ void pc_set(LCurve &L, double x, double P0, double P1, double C, bool
     __syncwarp();
 }
 // mapfindmax over the point cache's curvatures (first maximum under isless)
-__device__ int pc_argmax(const LCurve &L) {
+static __device__ int pc_argmax(const LCurve &L) {
     const int lane = threadIdx.x & 31;
     long long bk = 0;
     int bi = -1;
@@ -416,7 +475,7 @@ __device__ int pc_argmax(const LCurve &L) {
 }
 __device__ __forceinline__ double nrm2(double a, double b) { return sqrt(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b))); }
 // menger(Pj, Pk, Pl), src/lsqnonneg.jl:967-972
-__device__ double menger(double j0, double j1, double k0, double k1, double l0, double l1) {
+static __device__ double menger(double j0, double j1, double k0, double k1, double l0, double l1) {
     double djk0 = j0 - k0, djk1 = j1 - k1, dkl0 = k0 - l0, dkl1 = k1 - l1, dlj0 = l0 - j0, dlj1 = l1 - j1;
     double a = __dadd_rn(__dmul_rn(djk0, djk0), __dmul_rn(djk1, djk1));
     double b = __dadd_rn(__dmul_rn(dkl0, dkl0), __dmul_rn(dkl1, dkl1));
@@ -428,7 +487,7 @@ __device__ double menger(double j0, double j1, double k0, double k1, double l0, 
 // squared tolerances, and the curvature with one reciprocal square root (no
 // correctly rounded square roots and divisions on its dependency chain).
 __device__ __forceinline__ double sq2(double a, double b) { return fma(a, a, b * b); }
-__device__ double menger_fast(double j0, double j1, double k0, double k1, double l0, double l1) {
+static __device__ double menger_fast(double j0, double j1, double k0, double k1, double l0, double l1) {
     double djk0 = j0 - k0, djk1 = j1 - k1, dkl0 = k0 - l0, dkl1 = k1 - l1, dlj0 = l0 - j0, dlj1 = l1 - j1;
     double a = sq2(djk0, djk1), b = sq2(dkl0, dkl1), c = sq2(dlj0, dlj1);
     double cr = fma(djk0, dkl1, -(djk1 * dkl0));
@@ -440,7 +499,7 @@ struct LcState {
 // update_curvature!, src/lsqnonneg.jl:948-965.  The nearest cached
 // neighbours (largest key below x, smallest above; first index on ties) are
 // found lanes-over-entries with integer keys.
-__device__ void lc_update_curvature(LCurve &L, const LcState &s, const double *Ptl, const double *Pbr, double Ctol) {
+static __device__ void lc_update_curvature(LCurve &L, const LcState &s, const double *Ptl, const double *Pbr, double Ctol) {
     const int lane = threadIdx.x & 31;
     #pragma unroll 1
     for (int q = 0; q < 4; ++q) {
@@ -481,7 +540,7 @@ __device__ void lc_update_curvature(LCurve &L, const LcState &s, const double *P
 // width is <= the width of the state held so far; equivalently, k is adopted
 // iff it matches and its width is <= the running minimum over earlier matches
 // (and the current width).  Returns the last adopted index, or -1.
-__device__ int lc_backtrack(const LCurve &L, double xb, double w0) {
+static __device__ int lc_backtrack(const LCurve &L, double xb, double w0) {
     const int lane = threadIdx.x & 31;
     long long carry = __double_as_longlong(w0);  // widths are >= +0: bit order == value order
     int last = -1;
@@ -513,7 +572,7 @@ __device__ int lc_backtrack(const LCurve &L, double xb, double w0) {
     return last;
 }
 // lcurve_corner with backtracking, src/lsqnonneg.jl:872-919
-__device__ double lcurve_corner(LCurve &L, double xlow, double xhigh, double xtol, double Ptol, double Ctol) {
+static __device__ double lcurve_corner(LCurve &L, double xlow, double xhigh, double xtol, double Ptol, double Ctol) {
     const double PHI = 1.6180339887498949;
     L.flen = L.plen = L.slen = 0;
     L.overflow = false;
@@ -574,10 +633,10 @@ __device__ double lcurve_corner(LCurve &L, double xlow, double xhigh, double xto
     return L.px[pc_argmax(L)];
 }
 
-__device__ double *lcurve_scratch(Warp &w) { return w.scr + (long)w.P->m * w.P->n + 3L * w.P->K; }
+static __device__ double *lcurve_scratch(Warp &w) { return w.scr + (long)w.P->m * w.P->n + 3L * w.P->K; }
 
 // lsqnonneg_lcurve!, src/lsqnonneg.jl:812-840
-__device__ void reg_lcurve(Warp &w, double &mu_out, double &chi2_out) {
+static __device__ void reg_lcurve(Warp &w, double &mu_out, double &chi2_out) {
     double *base = lcurve_scratch(w);
     LCurve L;
     L.w = &w;
@@ -604,7 +663,7 @@ __device__ void reg_lcurve(Warp &w, double &mu_out, double &chi2_out) {
 // ---- GCV (src/lsqnonneg.jl:1136-1341) ----
 // Singular values of the m x n basis by one-sided Hestenes-Jacobi in shared
 // memory (stand-in for LAPACK dgesdd job 'N'), sorted descending into gam.
-__device__ void warp_svdvals(Warp &w, double *gam) {
+static __device__ void warp_svdvals(Warp &w, double *gam) {
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lane = w.lane;
     const int r = m >= n ? m : n, c = m >= n ? n : m;
@@ -695,7 +754,7 @@ struct GcvF {  // log𝒢(logμ), src/lsqnonneg.jl:1150-1154 and gcv!, 1213-1229
         return pm_log(jmax(G, low));
     }
 };
-__device__ void reg_gcv(Warp &w, double &mu_out, double &chi2_out) {
+static __device__ void reg_gcv(Warp &w, double &mu_out, double &chi2_out) {
     const Params &P = *w.P;
     double *gam = w.scr + (long)P.m * P.n + 3L * P.K + (long)kCacheCap * 19;
     if (!w.mixed) warp_svdvals(w, gam);  // the mixed method takes them from its Gram matrix (gram_svdvals)
@@ -732,7 +791,7 @@ struct Search {
 __device__ __forceinline__ bool sseen(const Search &S, int I) { return (S.seen[(I - 1) >> 5] >> ((I - 1) & 31)) & 1u; }
 
 // loss_with_grad!(prob, I), src/splines.jl:1010-1041
-__device__ void fa_update(Search &S, int I) {
+static __device__ void fa_update(Search &S, int I) {
     Warp &w = *S.w;
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lane = w.lane;
@@ -750,7 +809,7 @@ __device__ void fa_update(Search &S, int I) {
     double ell = __dmul_rn(r.rnorm, r.rnorm);
     double part = 0;
     #pragma unroll 1
-    for (int i0 = 0; i0 < m; i0 += 32) {
+    for (int i0 = 0; i0 < (kLegacyKernel && P.legacy ? 0 : m); i0 += 32) {  // legacy: loss! only, src/splines.jl:1043-1046
         int i = i0 + lane;
         double ax = 0, dax = 0;
         if (i < m) {
@@ -768,7 +827,7 @@ __device__ void fa_update(Search &S, int I) {
     double dt = wsum(part);
     if (lane == 0) {
         S.u[I - 1] = ell;
-        S.du[I - 1] = 2 * dt;
+        S.du[I - 1] = kLegacyKernel && P.legacy ? CUDART_NAN : 2 * dt;
         // insertsorted!(idx, I, npts += 1), src/utils.jl:42-49
         int len = S.npts + 1, val = I;
         #pragma unroll 1
@@ -782,7 +841,7 @@ __device__ void fa_update(Search &S, int I) {
     S.npts++;
 }
 // update!(surr, state, I; maxeval), src/splines.jl:736-744
-__device__ bool fa_state_update(Search &S, int I) {
+static __device__ bool fa_state_update(Search &S, int I) {
     if (S.numeval >= S.maxeval) return true;
     if (sseen(S, I)) return false;
     fa_update(S, I);
@@ -792,7 +851,7 @@ __device__ bool fa_state_update(Search &S, int I) {
 }
 __device__ __forceinline__ bool box_done(const Search &S, int lo, int hi) { return (int)sseen(S, lo) + (int)sseen(S, hi) >= 2; }
 // evaluate_box!, src/splines.jl:802-815
-__device__ void fa_evaluate_box(Search &S, int lo, int hi, bool have_x, double x) {
+static __device__ void fa_evaluate_box(Search &S, int lo, int hi, bool have_x, double x) {
     const double *g = S.w->P->angles;
     int c0 = lo, c1 = hi;
     if (have_x) {
@@ -806,7 +865,7 @@ __device__ void fa_evaluate_box(Search &S, int lo, int hi, bool have_x, double x
 }
 // initialize! (recursive breadth-limited bisection), src/splines.jl:716-734,
 // run with an explicit depth-first stack.
-__device__ void fa_initialize(Search &S) {
+static __device__ void fa_initialize(Search &S) {
     const int K = S.w->P->K;
     #pragma unroll 1
     for (int depth = 1; depth <= S.mineval; ++depth) {
@@ -830,7 +889,7 @@ __device__ void fa_initialize(Search &S) {
     }
 }
 // CubicHermiteInterpolator + minimize, src/splines.jl:62-110
-__device__ void hermite_minimize(double a, double b, double u0, double u1, double m0, double m1, double &xo, double &uo) {
+static __device__ void hermite_minimize(double a, double b, double u0, double u1, double m0, double m1, double &xo, double &uo) {
     double r = (b - a) / 2;
     m0 = r * m0; m1 = r * m1;
     double du = u1 - u0, dm = m1 - m0, su = u1 + u0, sm = m1 + m0;
@@ -856,8 +915,30 @@ __device__ void hermite_minimize(double a, double b, double u0, double u1, doubl
     uo = uend;
 }
 // suggest_point(::CubicHermiteSplineSurrogate), src/splines.jl:544-566
-__device__ void fa_suggest(Search &S, double &xo, double &uo) {
+// suggest_point(::CubicSplineSurrogate) with spline_opt_legacy,
+// src/splines.jl:493-500,419-431.  The scan depends only on the evaluated
+// points, so an unchanged set reuses it: the last suggestion (points, x, u)
+// is kept in the scratch words after the scan's workspace.
+static __device__ __noinline__ double2 fa_suggest_legacy(const double *angles, const double *u, const int *sidx, int npts,
+                                                  double *ws) {
+    double *memo = ws + legacy_ws_doubles(kLegacyMaxPts);
+    if (memo[0] != (double)npts) {
+        __syncwarp();
+        double2 r = legacy_scan(angles, u, sidx, npts, false, 0.0, ws);
+        if ((threadIdx.x & 31) == 0) { memo[0] = (double)npts; memo[1] = r.x; memo[2] = r.y; }
+        __syncwarp();
+        return r;
+    }
+    return make_double2(memo[1], memo[2]);
+}
+static __device__ void fa_suggest(Search &S, double &xo, double &uo) {
     const double *g = S.w->P->angles;
+    if (kLegacyKernel && S.w->P->legacy) {
+        double2 r = fa_suggest_legacy(g, S.u, S.sidx, S.npts, legacy_ws(*S.w));
+        xo = r.x;
+        uo = r.y;
+        return;
+    }
     int I0 = S.sidx[0];
     double pl = g[I0 - 1], ul = S.u[I0 - 1], dl = S.du[I0 - 1], p = pl, u = ul;
     #pragma unroll 1
@@ -872,7 +953,7 @@ __device__ void fa_suggest(Search &S, double &xo, double &uo) {
     uo = u;
 }
 // minimal_bounding_box, src/splines.jl:778-800
-__device__ void fa_min_bbox(const Search &S, double x, int &plo, int &phi) {
+static __device__ void fa_min_bbox(const Search &S, double x, int &plo, int &phi) {
     const double *g = S.w->P->angles;
     int lo = 1, hi = S.w->P->K;
     #pragma unroll 1
@@ -890,7 +971,7 @@ __device__ void fa_min_bbox(const Search &S, double x, int &plo, int &phi) {
     phi = hi;
 }
 // optimize_flip_angle!, src/T2mapSEcorr.jl:409-423 + bisection_search, src/splines.jl:750-775
-__device__ double flip_angle_search(Warp &w) {
+static __device__ double flip_angle_search(Warp &w) {
     const Params &P = *w.P;
     Search S;
     S.w = &w;
@@ -900,6 +981,7 @@ __device__ double flip_angle_search(Warp &w) {
     #pragma unroll 1
     for (int q = 0; q < 8; ++q) S.seen[q] = 0;
     S.npts = 0; S.numeval = 0; S.mineval = P.mineval; S.maxeval = P.maxeval;
+    if (kLegacyKernel && P.legacy && w.lane == 0) legacy_ws(w)[legacy_ws_doubles(kLegacyMaxPts)] = -1.0;  // no suggestion yet
     fa_initialize(S);
     double x, u;
     fa_suggest(S, x, u);
@@ -919,7 +1001,7 @@ __device__ double flip_angle_search(Warp &w) {
 // EPG basis at one angle: lanes over T2 columns, states in shared memory
 // (src/T2mapSEcorr.jl:275-283 with the default EPG kernels).
 // ----------------------------------------------------------------------------
-__device__ void warp_basis(Warp &w, double alpha, double *out /* m x n, global */) {
+static __device__ void warp_basis(Warp &w, double alpha, double *out /* m x n, global */) {
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lanes = P.epg_lanes, lane = w.lane;
     double *S = w.s.C;  // 3*m*lanes doubles, lane-contiguous
@@ -948,7 +1030,7 @@ __device__ void warp_basis(Warp &w, double alpha, double *out /* m x n, global *
 // (exactly, on the integer pipes) into w.A.  The basis of the voxel is these
 // FP32 values, for the Gram matrix and the fitted curve alike, and no FP32 <->
 // FP64 conversion occupies the FP64 pipe.
-__device__ void warp_basis_f32(Warp &w, double alpha) {
+static __device__ void warp_basis_f32(Warp &w, double alpha) {
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lanes = P.epg_lanes_f32, lane = w.lane;
     float *S = reinterpret_cast<float *>(w.g.G);  // 3*m*lanes floats, lane-contiguous
@@ -984,7 +1066,7 @@ __device__ void warp_basis_f32(Warp &w, double alpha) {
 // ----------------------------------------------------------------------------
 // One voxel (src/T2mapSEcorr.jl:201-238, save_results! 512-591, T2part 95-138)
 // ----------------------------------------------------------------------------
-__device__ void process_voxel(Warp &w, long v) {
+static __device__ void process_voxel(Warp &w, long v) {
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lane = w.lane;
     w.nsol = 0;
@@ -1047,7 +1129,10 @@ __device__ void process_voxel(Warp &w, long v) {
     }
     case 1: reg_lcurve(w, mu, chi2); break;
     case 2: reg_gcv(w, mu, chi2); break;
-    case 3: reg_chi2(w, P.chi2factor, mu, chi2); break;
+    case 3:
+        if (kLegacyKernel && P.legacy) reg_chi2_legacy(w, P.chi2factor, mu, chi2);
+        else reg_chi2(w, P.chi2factor, mu, chi2);
+        break;
     default: {
         double delta = sqrt((double)m) * (P.noiselevel / mx);
         reg_mdp(w, delta, mu, chi2);

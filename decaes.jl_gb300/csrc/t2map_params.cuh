@@ -36,6 +36,7 @@ struct Params {
     int epg_lanes;
     // mixed-precision method (normal-equation NNLS, FP32 EPG at the fitted angle)
     int mixed;
+    int legacy;         // legacy algorithms: spline surrogate search, chi2 doubling search
     const double *Gs;   // packed Gram matrices A_k'A_k of the grid bases (K x n(n+1)/2), or of the fixed basis
     const double *AsT;  // the grid (or fixed) bases transposed, K x m x n (row-major per basis)
     int epg_lanes_f32;  // lanes of the FP32 EPG (states in the Gram and factor regions)

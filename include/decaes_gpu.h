@@ -45,7 +45,7 @@ enum {
     DECAES_ECUDA = 2,    /* CUDA runtime error */
     DECAES_ENOMEM = 3,   /* allocation would exceed the context's HBM budget, or the
                             problem does not fit the no-allocation workspace */
-    DECAES_ELEGACY = 4,  /* legacy=true algorithms are not provided */
+    DECAES_ELEGACY = 4,  /* no longer returned (legacy = true is provided); value kept */
 };
 
 typedef struct decaes_ctx decaes_ctx;
@@ -72,7 +72,9 @@ typedef struct {
     int32_t SaveDecayCurve;
     int32_t SaveRegParam;
     int32_t SaveNNLSBasis;
-    int32_t legacy;       /* must be 0 */
+    int32_t legacy;       /* legacy algorithms: spline-surrogate angle search (spline_opt_legacy),
+                             chi2 by mu doubling + spline root (src/T2mapSEcorr.jl:401-403,
+                             src/lsqnonneg.jl:595-636) */
     int32_t precision;    /* DECAES_PREC_* (extension; not a reference field) */
 } decaes_t2map_opts;
 
@@ -96,7 +98,7 @@ typedef struct {
     double SPWin[2];
     double MPWin[2];
     double Sigmoid; /* NaN = nothing */
-    int32_t legacy; /* must be 0 */
+    int32_t legacy; /* accepted; T2part has no legacy-specific arithmetic */
 } decaes_t2part_opts;
 
 typedef struct {

@@ -1315,6 +1315,7 @@ static void reg_solve_tikh(reg_ws *r, double mu) {
 static inline double unreg_res2(const reg_ws *r) { return r->un.rnorm * r->un.rnorm; }
 static inline double tikh_res2(const reg_ws *r) { return tikh_resnorm_sq(&r->tk, r->tk_mu); }
 
+static void spline_root_legacy_pts(const double *X, const double *Y, int npts, double value, double *x);
 /* lsqnonneg_chi2!(method=:brent), src/lsqnonneg.jl:504-593 */
 static double chi2_f(double logmu, void *ctx) {
     reg_ws *r = (reg_ws *)ctx;
@@ -1360,6 +1361,47 @@ static const double *reg_chi2(reg_ws *r, double chi2_target, double *mu_out, dou
     *mu_out = mu;
     *chi2_out = res2 / res2_min;
     return r->tk.x;
+}
+
+/* lsqnonneg_chi2!(legacy = true), src/lsqnonneg.jl:504-531, with
+ * chi2_search_from_minimum(legacy = true), src/lsqnonneg.jl:595-636: double mu
+ * from 1e-3 until res2(mu) >= Chi2Factor * res2_min, then the legacy spline
+ * root through all (mu, res2) pairs including (0, res2_min).  Deviation: the
+ * doubling stops after CHI2_LEGACY_MAXDOUBLE steps (mu = 1e-3 * 2^20), where the
+ * reference would keep doubling without bound on data that never reaches the
+ * target. */
+#define CHI2_LEGACY_MAXDOUBLE 20
+static const double *reg_chi2_legacy(reg_ws *r, double chi2_target, double *mu_out, double *chi2_out) {
+    g_st = ORC_ST_REG_NNLS;
+    reg_solve_unreg(r);
+    g_st = ORC_ST_REG_OTHER;
+    double res2_min = unreg_res2(r);
+    if (res2_min == 0 || r->un.nsetp == 0) { *mu_out = 0; *chi2_out = 1; return r->un.x; }
+    double mus[CHI2_LEGACY_MAXDOUBLE + 2], r2s[CHI2_LEGACY_MAXDOUBLE + 2];
+    int cnt = 0;
+    mus[cnt] = 0; r2s[cnt++] = res2_min;
+    double munew = 1e-3;
+    for (int it = 0;; ++it) {
+        g_st = ORC_ST_REG_NNLS;
+        reg_solve_tikh(r, munew);
+        g_st = ORC_ST_REG_OTHER;
+        double res2new = tikh_res2(r);
+        mus[cnt] = munew; r2s[cnt++] = res2new;
+        if (res2new >= chi2_target * res2_min || it == CHI2_LEGACY_MAXDOUBLE) break;
+        munew *= 2.0;
+    }
+    double mu, res2;
+    spline_root_legacy_pts(mus, r2s, cnt, chi2_target * res2_min, &mu);
+    if (mu == 0) res2 = res2_min;
+    else {
+        g_st = ORC_ST_REG_NNLS;
+        reg_solve_tikh(r, mu);
+        g_st = ORC_ST_REG_OTHER;
+        res2 = tikh_res2(r);
+    }
+    *mu_out = mu;
+    *chi2_out = res2 / res2_min;
+    return mu == 0 ? r->un.x : r->tk.x;
 }
 
 /* lsqnonneg_mdp!, src/lsqnonneg.jl:700-747 */
@@ -1631,6 +1673,265 @@ static const double *reg_gcv(reg_ws *r, double *mu_out, double *chi2_out, int ne
     return r->tk.x;
 }
 
+#define LEGACY_MAXPTS 256
+/* ------------------------------------------------------------------------- */
+/* Legacy algorithms (T2mapOptions.legacy = true)                             */
+/*   - Julia's start:step:stop for Float64 (Base twiceprecision.jl, the       */
+/*     Julia 1.9 the reference targets): a StepRangeLen with a TwicePrecision */
+/*     reference and step;                                                    */
+/*   - Dierckx.Spline1D(x, y; k, bc = "extrapolate", s = 0) (src/splines.jl:  */
+/*     312-315), which calls netlib FITPACK: curfit/fpcurf with s = 0 (the    */
+/*     interpolating spline: Givens QR of the banded B-spline collocation     */
+/*     matrix, fpgivs/fprota/fpback) and splev/fpbspl (de Boor-Cox values);   */
+/*   - spline_opt_legacy / spline_root_legacy (src/splines.jl:417-446):       */
+/*     brute force over knots[1]:0.001:knots[end];                            */
+/*   - chi2_search_from_minimum(legacy = true) (src/lsqnonneg.jl:595-636).    */
+/* ------------------------------------------------------------------------- */
+typedef struct { double ref_hi, ref_lo, step_hi, step_lo; long offset, len; } jl_range;
+
+/* Base.mul12 and Base.canonicalize2 */
+static void jl_mul12(double x, double y, double *h, double *l) {
+    double p = x * y;
+    if (p == 0 || !isfinite(p)) { *h = p; *l = p; return; }
+    double e = fma(x, y, -p);
+    double s = p + e;
+    *h = s; *l = (p - s) + e;
+}
+/* TwicePrecision{Float64}((num, den)) = TwicePrecision(num) / den, for |num|, |den| < 2^53 */
+static void tp_ratio(long num, long den, double *hi, double *lo) {
+    double xh = (double)num, yh = (double)den;
+    double h = xh / yh, uh, ul;
+    jl_mul12(h, yh, &uh, &ul);
+    double l = ((((xh - uh) - ul) + 0.0) - h * 0.0) / yh;
+    if (xh == 0 || !isfinite(h)) { *hi = h; *lo = h; return; }
+    double s = h + l;
+    *hi = s; *lo = (h - s) + l;
+}
+static int isbetween(double a, double x, double b) { return (a <= x && x <= b) || (b <= x && x <= a); }
+static long lgcd_pos(long a, long b) { a = labs(a); b = labs(b); while (b) { long t = a % b; a = b; b = t; } return a; }
+
+/* (:)(start::Float64, step::Float64, stop::Float64) */
+static void jl_colon(double start, double step, double stop, jl_range *r) {
+    long step_n, step_d;
+    jl_rat(step, &step_n, &step_d);
+    if (step_d != 0 && (double)step_n / (double)step_d == step) {
+        long start_n, start_d, stop_n, stop_d;
+        jl_rat(start, &start_n, &start_d);
+        jl_rat(stop, &stop_n, &stop_d);
+        if (start_d != 0 && stop_d != 0 && (double)start_n / (double)start_d == start &&
+            (double)stop_n / (double)stop_d == stop) {
+            long g = lgcd_pos(start_d, step_d);
+            long den = g == 0 ? 0 : labs(start_d / g * step_d);
+            const double m = 9007199254740992.0; /* maxintfloat(Float64, Int) */
+            if (den != 0 && fabs(start * (double)den) <= m && fabs(step * (double)den) <= m &&
+                den % start_d == 0 && den % step_d == 0) {
+                long sn = (long)rint(start * (double)den), tn = (long)rint(step * (double)den);
+                long q = (den * stop_n - stop_d * sn + tn * stop_d) / (tn * stop_d); /* div truncates */
+                long len = q > 0 ? q : 0;
+                if (isbetween(start, start + (double)(len - 1) * step, stop + step / 2) &&
+                    !isbetween(start, start + (double)len * step, stop)) {
+                    /* floatrange(Float64, sn, tn, len, den) */
+                    long imin, ref_n;
+                    int nb;
+                    if (len < 2 || tn == 0) { imin = 1; ref_n = sn; nb = 0; }
+                    else {
+                        double t = rint(-(double)sn / (double)tn + 1);
+                        imin = t < 1 ? 1 : (t > (double)len ? len : (long)t);
+                        ref_n = sn + (imin - 1) * tn;
+                        nb = nbitslen((int)len, (int)imin);
+                    }
+                    tp_ratio(ref_n, den, &r->ref_hi, &r->ref_lo);
+                    double sh, sl;
+                    tp_ratio(tn, den, &sh, &sl);
+                    r->step_hi = truncbits(sh, nb);
+                    r->step_lo = (sh - r->step_hi) + sl;
+                    r->offset = imin;
+                    r->len = len;
+                    return;
+                }
+            }
+        }
+    }
+    /* fallback: start and step taken literally */
+    double lf = (stop - start) / step;
+    long len;
+    if (lf < 0) len = 0;
+    else if (lf == 0) len = 1;
+    else {
+        len = (long)rint(lf) + 1;
+        double stop2 = start + (double)(len - 1) * step;
+        len -= (start < stop && stop < stop2) + (start > stop && stop > stop2);
+    }
+    r->ref_hi = start; r->ref_lo = 0;
+    r->step_hi = step; r->step_lo = 0;
+    r->offset = 1;
+    r->len = len;
+}
+/* unsafe_getindex(::StepRangeLen{Float64, TwicePrecision, TwicePrecision}, i), 1-based */
+static inline double jl_range_at(const jl_range *r, long i) {
+    double u = (double)(i - r->offset);
+    double sh = u * r->step_hi, sl = u * r->step_lo, xh, xl;
+    add12(r->ref_hi, sh, &xh, &xl);
+    return xh + (xl + (sl + r->ref_lo));
+}
+int orc_jl_colon(double start, double step, double stop, double *out, long maxlen, long *len) {
+    jl_range r;
+    jl_colon(start, step, stop, &r);
+    *len = r.len;
+    for (long i = 1; i <= r.len && i <= maxlen; ++i) out[i - 1] = jl_range_at(&r, i);
+    return 0;
+}
+
+/* FITPACK fpbspl: the k+1 non-zero B-splines of degree k at t(l) <= x < t(l+1)
+ * (t and h 1-based). */
+static void fp_bspl(const double *t, int k, double x, int l, double *h) {
+    double hh[4];
+    h[1] = 1.0;
+    for (int j = 1; j <= k; ++j) {
+        for (int i = 1; i <= j; ++i) hh[i] = h[i];
+        h[1] = 0.0;
+        for (int i = 1; i <= j; ++i) {
+            int li = l + i, lj = li - j;
+            if (t[li] == t[lj]) { h[i + 1] = 0.0; continue; }
+            double f = hh[i] / (t[li] - t[lj]);
+            h[i] = h[i] + f * (t[li] - x);
+            h[i + 1] = f * (x - t[lj]);
+        }
+    }
+}
+/* FITPACK fpgivs / fprota */
+static void fp_givs(double piv, double *ww, double *c, double *s) {
+    double store = fabs(piv), dd;
+    if (store >= *ww) { double q = *ww / piv; dd = store * sqrt(1.0 + q * q); }
+    else { double q = piv / *ww; dd = *ww * sqrt(1.0 + q * q); }
+    *c = *ww / dd;
+    *s = piv / dd;
+    *ww = dd;
+}
+static inline void fp_rota(double c, double s, double *a, double *b) {
+    double s1 = *a, s2 = *b;
+    *b = c * s2 + s * s1;
+    *a = c * s1 - s * s2;
+}
+/* curfit(iopt = 0, s = 0, w = 1): the interpolating spline of degree k through
+ * (x(i), y(i)), i = 1..m (x increasing, m > k).  Writes the n = m + k + 1 knots
+ * t(1..n) and the m coefficients c(1..m) (1-based arrays of n + 1 entries);
+ * a and z are workspaces of (m + 1) * (k + 2) and m + 1 entries.  Returns n. */
+static int fp_curfit0(const double *x, const double *y, int m, int k, double *t, double *c, double *a, double *z) {
+    const int k1 = k + 1, k2 = k1 + 1, n = m + k1, nk1 = n - k1;
+    /* interior knots of the interpolating spline */
+    int mk1 = m - k1;
+    if (mk1 > 0) {
+        int k3 = k / 2, i = k2, j = k3 + 2;
+        if (k3 * 2 != k) for (int l = 1; l <= mk1; ++l, ++i, ++j) t[i] = x[j];
+        else for (int l = 1; l <= mk1; ++l, ++i, ++j) t[i] = (x[j] + x[j - 1]) * 0.5;
+    }
+    for (int j = 1, i = n; j <= k1; ++j, --i) { t[j] = x[1]; t[i] = x[m]; }
+    /* observation matrix reduced to upper triangular form by Givens rotations */
+#define FA(i, j) a[(i) * (k2) + (j)]
+    for (int i = 1; i <= nk1; ++i) { z[i] = 0; for (int j = 1; j <= k1; ++j) FA(i, j) = 0; }
+    int l = k1;
+    double h[5];
+    for (int it = 1; it <= m; ++it) {
+        double xi = x[it], yi = y[it];
+        while (!(xi < t[l + 1] || l == nk1)) l++;
+        fp_bspl(t, k, xi, l, h);
+        int j = l - k1;
+        for (int i = 1; i <= k1; ++i) {
+            j++;
+            double piv = h[i];
+            if (piv == 0) continue;
+            double cs, sn;
+            fp_givs(piv, &FA(j, 1), &cs, &sn);
+            fp_rota(cs, sn, &yi, &z[j]);
+            if (i == k1) break;
+            for (int i1 = i + 1, i2 = 1; i1 <= k1; ++i1) {
+                i2++;
+                fp_rota(cs, sn, &h[i1], &FA(j, i2));
+            }
+        }
+    }
+    /* fpback(a, z, nk1, k1, c): back substitution, bandwidth k1 */
+    c[nk1] = z[nk1] / FA(nk1, 1);
+    int i = nk1 - 1;
+    for (int j = 2; j <= nk1 && i >= 1; ++j, --i) {
+        double store = z[i];
+        int i1 = (j <= k) ? j - 1 : k, mm = i;
+        for (int q = 1; q <= i1; ++q) { mm++; store = store - c[mm] * FA(i, q + 1); }
+        c[i] = store / FA(i, 1);
+    }
+#undef FA
+    return n;
+}
+/* splev for one point, bc = "extrapolate" (e = 0) */
+static double fp_splev1(const double *t, int n, const double *c, int k, double arg) {
+    const int k1 = k + 1, nk1 = n - k1;
+    int l = k1;
+    while (!(arg < t[l + 1] || l == nk1)) l++;
+    double h[5];
+    fp_bspl(t, k, arg, l, h);
+    double sp = 0;
+    for (int j = 1, ll = l - k1; j <= k1; ++j) { ll++; sp = sp + c[ll] * h[j]; }
+    return sp;
+}
+int orc_fitpack_curfit0(const double *x, const double *y, int m, int k, double *t, double *c) {
+    if (m <= k || k < 1 || k > 3) return 1;
+    double *xs = (double *)calloc((size_t)(m + 1) * 2, sizeof(double)), *ys = xs + m + 1;
+    double *tt = (double *)calloc((size_t)(m + k + 2) * 2, sizeof(double)), *cc = tt + m + k + 2;
+    double *a = (double *)calloc((size_t)(m + 1) * (k + 2), sizeof(double)), *z = (double *)calloc(m + 1, sizeof(double));
+    for (int i = 0; i < m; ++i) { xs[i + 1] = x[i]; ys[i + 1] = y[i]; }
+    int n = fp_curfit0(xs, ys, m, k, tt, cc, a, z);
+    for (int i = 0; i < n; ++i) t[i] = tt[i + 1];
+    for (int i = 0; i < m; ++i) c[i] = cc[i + 1];
+    free(xs); free(tt); free(a); free(z);
+    return 0;
+}
+int orc_fitpack_splev(const double *t, int n, const double *c, int k, const double *x, int npts, double *y) {
+    double *tt = (double *)malloc(sizeof(double) * (n + 1) * 2), *cc = tt + n + 1;
+    for (int i = 0; i < n; ++i) { tt[i + 1] = t[i]; cc[i + 1] = i < n - k - 1 ? c[i] : 0; }
+    for (int i = 0; i < npts; ++i) y[i] = fp_splev1(tt, n, cc, k, x[i]);
+    free(tt);
+    return 0;
+}
+
+/* Shared core of spline_opt_legacy (value = NaN: minimize the spline) and
+ * spline_root_legacy (minimize |spline - value|): fit with
+ * deg_spline = min(3, npts - 1), then scan knots[1]:0.001:knots[end] keeping
+ * the first strict minimum.  X, Y are 0-based of length npts.  */
+static void spline_scan_legacy(const double *X, const double *Y, int npts, int root, double value, double *xo, double *yo) {
+    int k = npts - 1 < 3 ? npts - 1 : 3;
+    double xs[LEGACY_MAXPTS + 1], ys[LEGACY_MAXPTS + 1], t[LEGACY_MAXPTS + 5], c[LEGACY_MAXPTS + 5];
+    double a[(LEGACY_MAXPTS + 1) * 5], z[LEGACY_MAXPTS + 1];
+    for (int i = 0; i < npts; ++i) { xs[i + 1] = X[i]; ys[i + 1] = Y[i]; }
+    int n = fp_curfit0(xs, ys, npts, k, t, c, a, z);
+    jl_range r;
+    jl_colon(t[k + 1], 0.001, t[n - k], &r);  /* get_knots: t[k+1 .. n-k] */
+    double bx = jl_range_at(&r, 1), by = fp_splev1(t, n, c, k, bx);
+    if (root) by = fabs(by - value);
+    for (long i = 2; i <= r.len; ++i) {
+        double xi = jl_range_at(&r, i), yi = fp_splev1(t, n, c, k, xi);
+        if (root) yi = fabs(yi - value);
+        if (yi < by) { bx = xi; by = yi; }
+    }
+    *xo = bx;
+    *yo = by;
+}
+int orc_spline_opt_legacy(const double *X, const double *Y, int npts, double *x, double *y) {
+    if (npts < 2 || npts > LEGACY_MAXPTS) return 1;
+    spline_scan_legacy(X, Y, npts, 0, 0.0, x, y);
+    return 0;
+}
+static void spline_root_legacy_pts(const double *X, const double *Y, int npts, double value, double *x) {
+    double y;
+    spline_scan_legacy(X, Y, npts, 1, value, x, &y);
+}
+int orc_spline_root_legacy(const double *X, const double *Y, int npts, double value, double *x) {
+    if (npts < 2 || npts > LEGACY_MAXPTS) return 1;
+    double y;
+    spline_scan_legacy(X, Y, npts, 1, value, x, &y);
+    return 0;
+}
+
 /* ------------------------------------------------------------------------- */
 /* Flip-angle search (src/splines.jl, src/T2mapSEcorr.jl:409-423)             */
 /* ------------------------------------------------------------------------- */
@@ -1677,6 +1978,9 @@ typedef struct {
     unsigned char seen[256];
     double u[256], du[256];
     int idx[256], npts, numeval, maxeval, mineval;
+    int legacy;                     /* CubicSplineSurrogate(legacy = true): loss only, brute-force spline minimum */
+    int sugg_npts;                  /* points behind the last legacy suggestion (-1: none) */
+    double sugg_x, sugg_u;
 } fa_search;
 
 /* loss_with_grad!, src/splines.jl:1010-1041 */
@@ -1689,6 +1993,7 @@ static void fa_update(fa_search *s, int I) {
     g_st = ORC_ST_SEARCH_OTHER;
     double ell = s->un->rnorm * s->un->rnorm;
     const double *x = s->un->x;
+    if (s->legacy) { s->du[I - 1] = NAN; goto store; } /* loss! only, src/splines.jl:1043-1046 */
     for (int i = 0; i < m; ++i) s->Axb[i] = 0;
     for (int j = 0; j < n; ++j)
         if (x[j] > 0) { for (int i = 0; i < m; ++i) s->Axb[i] = fma(x[j], A[i + (size_t)j * m], s->Axb[i]); FL(2 * m); }
@@ -1700,9 +2005,10 @@ static void fa_update(fa_search *s, int I) {
     for (int i = 0; i < m; ++i) Lg.p[i & 31] = fma(s->dAx[i], s->Axb[i], Lg.p[i & 31]);
     double dt = lacc_tree(&Lg);
     FL(3 * m + 2);
+    s->du[I - 1] = 2 * dt;
+store:
     s->seen[I - 1] = 1;
     s->u[I - 1] = ell;
-    s->du[I - 1] = 2 * dt;
     /* insertsorted!(idx, I, npts += 1), src/utils.jl:42-49 */
     int len = ++s->npts, val = I;
     for (int i = 0; i < len - 1; ++i) {
@@ -1745,6 +2051,18 @@ static void fa_init_rec(fa_search *s, unsigned char *sseen, int lo, int hi, int 
 }
 /* suggest_point(::CubicHermiteSplineSurrogate), src/splines.jl:544-566 */
 static void fa_suggest(fa_search *s, double *xo, double *uo) {
+    if (s->legacy) {
+        /* suggest_point(::CubicSplineSurrogate) with spline_opt_legacy, src/splines.jl:493-500,419-431.
+         * The scan depends only on the evaluated points, so an unchanged set reuses it. */
+        if (s->sugg_npts != s->npts) {
+            double ps[256], us[256];
+            for (int i = 0; i < s->npts; ++i) { ps[i] = s->grid[s->idx[i] - 1]; us[i] = s->u[s->idx[i] - 1]; }
+            spline_scan_legacy(ps, us, s->npts, 0, 0.0, &s->sugg_x, &s->sugg_u);
+            s->sugg_npts = s->npts;
+        }
+        *xo = s->sugg_x; *uo = s->sugg_u;
+        return;
+    }
     int I0 = s->idx[0];
     double pl = s->grid[I0 - 1], ul = s->u[I0 - 1], dl = s->du[I0 - 1];
     double p = pl, u = ul;
@@ -1781,7 +2099,7 @@ static double fa_optimize(fa_search *s, int mineval, int maxeval) {
     unsigned char sseen[256];
     memset(sseen, 0, sizeof sseen);
     memset(s->seen, 0, sizeof s->seen);
-    s->npts = 0; s->numeval = 0; s->mineval = mineval; s->maxeval = maxeval;
+    s->npts = 0; s->numeval = 0; s->mineval = mineval; s->maxeval = maxeval; s->sugg_npts = -1;
     for (int depth = 1; depth <= mineval; ++depth) {
         fa_init_rec(s, sseen, 1, s->K, depth);
         if (s->numeval >= mineval) break;
@@ -1838,6 +2156,7 @@ static void vox_ws_init(vox_ws *w, const t2map_plan *p) {
     w->fa.K = p->K; w->fa.m = m; w->fa.n = n;
     w->fa.grid = p->angles; w->fa.As = p->As; w->fa.dAs = p->dAs; w->fa.b = w->b;
     w->fa.un = &w->search_un;
+    w->fa.legacy = p->o.legacy;
     w->fa.Axb = (double *)calloc(m, sizeof(double));
     w->fa.dAx = (double *)calloc(m, sizeof(double));
 }
@@ -1879,7 +2198,9 @@ static void voxel(const t2map_plan *p, vox_ws *w, const double *image, long V, l
         break;
     case ORC_REG_LCURVE: x = reg_lcurve(&w->reg, &mu, &chi2f, need_chi2); break;
     case ORC_REG_GCV: x = reg_gcv(&w->reg, &mu, &chi2f, need_chi2); break;
-    case ORC_REG_CHI2: x = reg_chi2(&w->reg, o->Chi2Factor, &mu, &chi2f); break;
+    case ORC_REG_CHI2:
+        x = o->legacy ? reg_chi2_legacy(&w->reg, o->Chi2Factor, &mu, &chi2f) : reg_chi2(&w->reg, o->Chi2Factor, &mu, &chi2f);
+        break;
     default: {
         double sigma = o->NoiseLevel / mx;
         double delta = sqrt((double)m) * sigma;
@@ -2112,6 +2433,9 @@ int orc_lsqnonneg_tikh(const double *A, int m, int n, const double *b, double mu
     return 0;
 int orc_lsqnonneg_chi2(const double *A, int m, int n, const double *b, double chi2_target, double *x, double *mu, double *chi2) {
     REG_ENTRY(reg_chi2(&r, chi2_target, mu, chi2))
+}
+int orc_lsqnonneg_chi2_legacy(const double *A, int m, int n, const double *b, double chi2_target, double *x, double *mu, double *chi2) {
+    REG_ENTRY(reg_chi2_legacy(&r, chi2_target, mu, chi2))
 }
 int orc_lsqnonneg_mdp(const double *A, int m, int n, const double *b, double delta, double *x, double *mu, double *chi2) {
     REG_ENTRY(reg_mdp(&r, delta, mu, chi2, zero_n))

@@ -43,6 +43,7 @@ typedef struct {
     double NoiseLevel;
     double RefConAngle;
     double SetFlipAngle;
+    int legacy;          /* legacy algorithms: spline surrogate, chi2 doubling search */
 } orc_t2map_opts;
 
 /* Output buffers of T2mapSEcorr (src/T2mapSEcorr.jl:2-19); NULL = not saved.
@@ -109,6 +110,15 @@ int orc_lsqnonneg_mdp(const double *A, int m, int n, const double *b, double del
 int orc_lsqnonneg_lcurve(const double *A, int m, int n, const double *b, double *x, double *mu, double *chi2);
 int orc_lsqnonneg_gcv(const double *A, int m, int n, const double *b, double *x, double *mu, double *chi2);
 int orc_svdvals(const double *A, int m, int n, double *s);
+int orc_lsqnonneg_chi2_legacy(const double *A, int m, int n, const double *b, double chi2_target,
+                              double *x, double *mu, double *chi2);
+
+/* legacy spline machinery (FITPACK restatement, Julia float ranges) */
+int orc_jl_colon(double start, double step, double stop, double *out, long maxlen, long *len);
+int orc_fitpack_curfit0(const double *x, const double *y, int m, int k, double *t, double *c);
+int orc_fitpack_splev(const double *t, int n, const double *c, int k, const double *x, int npts, double *y);
+int orc_spline_opt_legacy(const double *X, const double *Y, int npts, double *x, double *y);
+int orc_spline_root_legacy(const double *X, const double *Y, int npts, double value, double *x);
 
 /* ---- scalar optimizers with a callback ---- */
 typedef double (*orc_fn)(double x, void *ctx);

@@ -34,7 +34,7 @@ class _T2mapOpts(C.Structure):
         ("T1", C.c_double), ("Threshold", C.c_double), ("MinRefAngle", C.c_double),
         ("nRefAngles", C.c_int), ("nRefAnglesMin", C.c_int), ("Reg", C.c_int),
         ("Chi2Factor", C.c_double), ("NoiseLevel", C.c_double), ("RefConAngle", C.c_double),
-        ("SetFlipAngle", C.c_double),
+        ("SetFlipAngle", C.c_double), ("legacy", C.c_int),
     ]
 
 
@@ -95,6 +95,12 @@ def lib():
         L.orc_lcurve_corner.restype = C.c_double
         L.orc_cubic_hermite_minimize.argtypes = [C.c_double] * 6 + [_dp, _dp]
         L.orc_minimal_bounding_box.argtypes = [C.c_int, _dp, C.POINTER(C.c_ubyte), C.c_double, _ip, _ip]
+        L.orc_lsqnonneg_chi2_legacy.argtypes = [_dp, C.c_int, C.c_int, _dp, C.c_double, _dp, _dp, _dp]
+        L.orc_jl_colon.argtypes = [C.c_double, C.c_double, C.c_double, _dp, C.c_long, C.POINTER(C.c_long)]
+        L.orc_fitpack_curfit0.argtypes = [_dp, _dp, C.c_int, C.c_int, _dp, _dp]
+        L.orc_fitpack_splev.argtypes = [_dp, C.c_int, _dp, C.c_int, _dp, C.c_int, _dp]
+        L.orc_spline_opt_legacy.argtypes = [_dp, _dp, C.c_int, _dp, _dp]
+        L.orc_spline_root_legacy.argtypes = [_dp, _dp, C.c_int, C.c_double, _dp]
         _lib = L
     return _lib
 
@@ -187,6 +193,53 @@ def lsqnonneg_chi2(A, b, chi2_target):
     return _reg(lib().orc_lsqnonneg_chi2, A, b, chi2_target)
 
 
+def lsqnonneg_chi2_legacy(A, b, chi2_target):
+    """lsqnonneg_chi2!(work, chi2_target, legacy = true)."""
+    return _reg(lib().orc_lsqnonneg_chi2_legacy, A, b, chi2_target)
+
+
+def jl_colon(start, step, stop, maxlen=None):
+    """collect(start:step:stop) for Float64 (Julia's TwicePrecision ranges)."""
+    n = C.c_long(0)
+    lib().orc_jl_colon(start, step, stop, None, 0, C.byref(n))
+    out = np.empty(n.value if maxlen is None else min(maxlen, n.value))
+    lib().orc_jl_colon(start, step, stop, _p(out), out.size, C.byref(n))
+    return out
+
+
+def fitpack_curfit0(x, y, k):
+    """Dierckx.Spline1D(x, y; k, s = 0): (knots t, coefficients c) as FITPACK's curfit."""
+    x, y = _f64(x), _f64(y)
+    m = x.size
+    t, c = np.empty(m + k + 1), np.empty(m)
+    if lib().orc_fitpack_curfit0(_p(x), _p(y), m, k, _p(t), _p(c)) != 0:
+        raise ValueError("curfit0 needs 1 <= k <= 3 < m")
+    return t, c
+
+
+def fitpack_splev(t, c, k, x):
+    t, c, x = _f64(t), _f64(c), _f64(x)
+    y = np.empty(x.size)
+    lib().orc_fitpack_splev(_p(t), t.size, _p(c), k, _p(x), x.size, _p(y))
+    return y
+
+
+def spline_opt_legacy(X, Y):
+    X, Y = _f64(X), _f64(Y)
+    x, y = C.c_double(), C.c_double()
+    if lib().orc_spline_opt_legacy(_p(X), _p(Y), X.size, C.byref(x), C.byref(y)) != 0:
+        raise ValueError("spline_opt_legacy: 2..256 points")
+    return x.value, y.value
+
+
+def spline_root_legacy(X, Y, value=0.0):
+    X, Y = _f64(X), _f64(Y)
+    x = C.c_double()
+    if lib().orc_spline_root_legacy(_p(X), _p(Y), X.size, value, C.byref(x)) != 0:
+        raise ValueError("spline_root_legacy: 2..256 points")
+    return x.value
+
+
 def lsqnonneg_mdp(A, b, delta):
     return _reg(lib().orc_lsqnonneg_mdp, A, b, delta)
 
@@ -272,6 +325,7 @@ class T2mapOptions:
     SaveResidualNorm: bool = False
     SaveDecayCurve: bool = False
     SaveRegParam: bool = False
+    legacy: bool = False
 
 
 def _nan(v):
@@ -286,8 +340,10 @@ def t2map(image, o: T2mapOptions, b1map=None, nthreads: int = 1, return_flops: b
     flat = np.asfortranarray(img, dtype=np.float64).reshape((V, m), order="F")
     flat = np.asfortranarray(flat)
     co = _T2mapOpts(m, o.TE, o.nT2, (C.c_double * 2)(*o.T2Range), o.T1, o.Threshold, o.MinRefAngle,
-                    o.nRefAngles, o.nRefAnglesMin if o.nRefAnglesMin is not None else min(5, o.nRefAngles),
-                    REG[o.Reg], _nan(o.Chi2Factor), _nan(o.NoiseLevel), o.RefConAngle, _nan(o.SetFlipAngle))
+                    o.nRefAngles, o.nRefAnglesMin if o.nRefAnglesMin is not None else
+                    (o.nRefAngles if o.legacy else min(5, o.nRefAngles)),
+                    REG[o.Reg], _nan(o.Chi2Factor), _nan(o.NoiseLevel), o.RefConAngle, _nan(o.SetFlipAngle),
+                    int(o.legacy))
     outs = {k: np.full(V, np.nan) for k in ("gdn", "ggm", "gva", "fnr", "snr", "alpha")}
     dist = np.full((V, o.nT2), np.nan, order="F")
     if o.SaveResidualNorm:

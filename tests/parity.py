@@ -15,7 +15,7 @@ def orc_opts(orc, o):
                             nRefAnglesMin=o.nRefAnglesMin, Chi2Factor=o.Chi2Factor, NoiseLevel=o.NoiseLevel,
                             RefConAngle=o.RefConAngle, SetFlipAngle=o.SetFlipAngle,
                             SaveResidualNorm=o.SaveResidualNorm, SaveDecayCurve=o.SaveDecayCurve,
-                            SaveRegParam=o.SaveRegParam)
+                            SaveRegParam=o.SaveRegParam, legacy=o.legacy)
 
 
 def dist_rel_err(d_gpu, d_orc):

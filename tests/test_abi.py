@@ -68,10 +68,12 @@ def test_option_defaults(D):
     assert p.MatrixSize == o.MatrixSize and p.nT2 == o.nT2 and p.T2Range == o.T2Range and p.Sigmoid is None
 
 
-def test_legacy_rejected(D):
-    with pytest.raises(AssertionError) as e:
-        D.T2mapOptions(**base(legacy=True))
-    assert "legacy" in str(e.value)
+def test_legacy_accepted(D):
+    """legacy = true is validated like any other option set (src/types.jl:59-63 defaults)."""
+    o = D.T2mapOptions(**base(legacy=True))
+    assert o.legacy and o.nRefAngles == 8 and o.nRefAnglesMin == 8
+    p = D.T2partOptions.from_t2map(o, SPWin=(10e-3, 25e-3), MPWin=(25e-3, 200e-3))
+    assert p.legacy
 
 
 @pytest.mark.parametrize("kw,msg", [

@@ -21,6 +21,9 @@ VOLS = [
     dict(X=(5, 5, 2), m=24, TE=12e-3, n=40, K=8, Reg="none", prec="fp64", dtype=np.float32, seed=3),
     dict(X=(4, 6, 2), m=56, TE=7e-3, n=60, K=64, Reg="gcv", prec="mixed", dtype=np.float64, bg=0.5, thr=200.0, seed=4),
     dict(X=(3, 3, 1), m=32, TE=10e-3, n=40, K=8, Reg="lcurve", prec="fp64", dtype=np.float32, seed=5, Sigmoid=5e-3),
+    # legacy = true: the batch runs on the legacy kernel, the other volumes with it
+    dict(X=(4, 4, 2), m=32, TE=10e-3, n=40, K=8, Reg="chi2", Chi2Factor=1.02, prec="fp64", dtype=np.float64, seed=6,
+         legacy=True),
 ]
 
 
@@ -38,7 +41,7 @@ class Vol:
         self.mo = D.T2mapOptions(MatrixSize=c["X"], nTE=c["m"], TE=c["TE"], nT2=c["n"], T2Range=(10e-3, 2.0),
                                  Reg=c["Reg"], nRefAngles=c["K"], Chi2Factor=c.get("Chi2Factor"),
                                  Threshold=c.get("thr", 0.0), SaveRegParam=True, SaveResidualNorm=True,
-                                 precision=c["prec"])
+                                 precision=c["prec"], legacy=c.get("legacy", False))
         self.po = D.T2partOptions.from_t2map(self.mo, SPWin=SPWIN, MPWin=MPWIN, Sigmoid=c.get("Sigmoid"))
         self.d_img = torch.from_numpy(np.asfortranarray(img).reshape(-1, order="F").copy()).cuda()
         V = int(np.prod(c["X"]))
@@ -98,7 +101,7 @@ def test_batch_matches_single_calls(D, ctx):
 
 def test_prepared_batch_replays(D, ctx):
     import torch
-    vols = [Vol(D, c) for c in VOLS[:3]]
+    vols = [Vol(D, c) for c in VOLS[:3]] + [Vol(D, VOLS[5])]
     want = []
     for v in vols:
         want.append(_single(D, ctx, v))

@@ -15,6 +15,9 @@ REQS = [
     dict(X=(5, 5, 1), m=56, TE=7e-3, n=60, K=64, Reg="gcv", prec="mixed", dtype=np.float32, seed=3),
     dict(X=(9, 9, 1), m=24, TE=12e-3, n=40, K=8, Reg="none", prec="fp64", dtype=np.float32, seed=4),
     dict(X=(6, 6, 2), m=48, TE=10e-3, n=40, K=32, Reg="lcurve", prec="fp64", dtype=np.float64, seed=5),
+    # legacy = true: ticks holding its chunks run the legacy kernel
+    dict(X=(5, 4, 2), m=32, TE=10e-3, n=40, K=8, Reg="chi2", Chi2Factor=1.02, prec="fp64", dtype=np.float32, seed=6,
+         legacy=True),
 ]
 
 
@@ -23,7 +26,7 @@ def _req(D, c):
                                           BackgroundFraction=c.get("bg", 0.0)), seed=c["seed"], dtype=c["dtype"])
     mo = D.T2mapOptions(MatrixSize=c["X"], nTE=c["m"], TE=c["TE"], nT2=c["n"], T2Range=(10e-3, 2.0), Reg=c["Reg"],
                         nRefAngles=c["K"], Chi2Factor=c.get("Chi2Factor"), Threshold=c.get("thr", 0.0),
-                        SaveRegParam=True, SaveResidualNorm=True, precision=c["prec"])
+                        SaveRegParam=True, SaveResidualNorm=True, precision=c["prec"], legacy=c.get("legacy", False))
     po = D.T2partOptions.from_t2map(mo, SPWin=SPWIN, MPWin=MPWIN)
     return img, mo, po
 
