@@ -1,0 +1,47 @@
+"""The command-line front end on the GPU: a NIfTI image through
+`python -m decaes_gb300`-style arguments gives, in its .mat outputs, exactly
+the arrays of the direct API call on the same image (and a B1 map file is
+used as the flip angles)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_cli_matches_api(D, ctx, tmp_path):
+    io = pytest.importorskip("scipy.io")
+    from decaes_gb300 import cli, nifti
+    X = (6, 5, 2)
+    img = D.mock_image(D.MockImageOptions(MatrixSize=X, nTE=32, TE=10e-3, BackgroundFraction=0.3), seed=8)
+    nifti.write(str(tmp_path / "mese.nii.gz"), img)
+    args = [str(tmp_path / "mese.nii.gz"), "--T2map", "--T2part", "--TE", "10e-3", "--nT2", "40", "--T2Range", "10e-3",
+            "2.0", "--SPWin", "10e-3", "25e-3", "--MPWin", "25e-3", "200e-3", "--Reg", "lcurve", "--nRefAngles", "16",
+            "--Threshold", "200", "--SaveRegParam", "-o", str(tmp_path / "out"), "--quiet"]
+    cli.run_main(args, ctx=ctx)
+    mo = D.T2mapOptions(MatrixSize=X, nTE=32, TE=10e-3, nT2=40, T2Range=(10e-3, 2.0), Reg="lcurve", nRefAngles=16,
+                        Threshold=200.0, SaveRegParam=True)
+    po = D.T2partOptions.from_t2map(mo, SPWin=(10e-3, 25e-3), MPWin=(25e-3, 200e-3))
+    maps, dist, parts = D.T2mapSEcorr_T2partSEcorr(np.asfortranarray(img, dtype=np.float64), mo, po, ctx=ctx)
+    d = io.loadmat(str(tmp_path / "out" / "mese.t2dist.mat"))["dist"]
+    np.testing.assert_array_equal(d, dist)
+    m = io.loadmat(str(tmp_path / "out" / "mese.t2maps.mat"))
+    for k in ("gdn", "ggm", "gva", "fnr", "snr", "alpha", "mu", "chi2factor"):
+        np.testing.assert_array_equal(m[k], maps[k], err_msg=k)
+    p = io.loadmat(str(tmp_path / "out" / "mese.t2parts.mat"))
+    for k in ("sfr", "sgm", "mfr", "mgm"):
+        np.testing.assert_array_equal(p[k], parts[k], err_msg=k)
+    assert np.isfinite(d).any()
+
+
+def test_cli_b1map(D, ctx, tmp_path):
+    io = pytest.importorskip("scipy.io")
+    from decaes_gb300 import cli, nifti
+    X = (4, 4, 1)
+    img = D.mock_image(D.MockImageOptions(MatrixSize=X, nTE=32, TE=10e-3), seed=9)
+    b1 = np.random.default_rng(5).uniform(150, 180, size=X)
+    nifti.write(str(tmp_path / "mese.nii"), img)
+    nifti.write(str(tmp_path / "b1.nii"), b1)
+    cli.run_main([str(tmp_path / "mese.nii"), "--T2map", "--TE", "10e-3", "--nT2", "40", "--T2Range", "10e-3", "2.0",
+                  "--Reg", "none", "--B1map", str(tmp_path / "b1.nii"), "--quiet"], ctx=ctx)
+    m = io.loadmat(str(tmp_path / "mese.t2maps.mat"))
+    np.testing.assert_array_equal(m["alpha"], b1)
