@@ -132,8 +132,11 @@ __global__ void k_compact_range(const void *image, int f32, long v0, long v1, do
 
 __global__ void __launch_bounds__(128) k_voxels(const __grid_constant__ Params P) { voxels_body(P); }
 __global__ void __launch_bounds__(128) k_voxels_batch(const __grid_constant__ BatchParams B) { voxels_batch_body(B); }
-// the same kernels with the legacy algorithms (decaes_legacy.cu)
+// the same kernels with the legacy algorithms (decaes_legacy.cu), and with one
+// method each (decaes_plain.cu, decaes_mixed.cu)
 __global__ void __launch_bounds__(128) k_voxels_legacy(const __grid_constant__ Params P);
+__global__ void __launch_bounds__(128) k_voxels_plain(const __grid_constant__ Params P);
+__global__ void __launch_bounds__(128) k_voxels_mixed(const __grid_constant__ Params P);
 __global__ void __launch_bounds__(128) k_voxels_batch_legacy(const __grid_constant__ BatchParams B);
 
 // offsets[0] = 0, offsets[v + 1] = offsets[v] + counts[v] (one thread; nvol is small).
@@ -498,7 +501,7 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
     P.smem_stride = wsm;
     int wpb = tuned_wpb(ctx, o), grid = 0;
     size_t smem = 0;
-    auto kern = o.legacy ? dk::k_voxels_legacy : dk::k_voxels;
+    auto kern = o.legacy ? dk::k_voxels_legacy : (o.precision == DECAES_PREC_MIXED ? dk::k_voxels_mixed : dk::k_voxels_plain);
     if (int rc = launch_shape(ctx, kern, wsm, &wpb, &grid, &smem)) return rc;
     void *scr;
     if (int rc = buf(ctx, "scratch", sizeof(double) * (size_t)P.scr_stride * grid * wpb, &scr)) return rc;

@@ -37,7 +37,7 @@ __global__ void k_basis_fixed(int m, int n, double alpha, double TE, double T1, 
                               const double *t2, double *A, double *work);
 __global__ void k_fill(double *p, long len, double v);
 __global__ void k_compact(const void *image, int f32, long V, double thr, int *vidx, int *nvox);
-__global__ void __launch_bounds__(128) k_voxels(const __grid_constant__ Params P);
+__global__ void __launch_bounds__(128) k_voxels_plain(const __grid_constant__ Params P);
 __global__ void __launch_bounds__(128) k_voxels_legacy(const __grid_constant__ Params P);
 }  // namespace dk
 
@@ -184,7 +184,7 @@ extern "C" int decaes_t2map_t2part_noalloc(const decaes_t2map_opts *mopts, const
                     "problem needs " + std::to_string(need_min) + " bytes of the " + std::to_string(kStaticBytes) +
                         "-byte static workspace (grows with the voxel count, nTE*nT2*nRefAngles and nT2); "
                         "split the image into smaller slabs");
-    auto kern = o.legacy ? dk::k_voxels_legacy : dk::k_voxels;
+    auto kern = o.legacy ? dk::k_voxels_legacy : dk::k_voxels_plain;
     NA_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     NA_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem));

@@ -11,14 +11,22 @@
 
 // The legacy algorithms are compiled only into the kernels of the translation
 // unit that defines DECAES_LEGACY_KERNEL=1; elsewhere kLegacyKernel is false
-// and the legacy branches fold away.
+// and the legacy branches fold away.  Likewise DECAES_METHODS selects the
+// least-squares methods a translation unit's kernels carry (1 the plain FP64
+// method, 2 the mixed method, 3 both, chosen per volume at run time): a kernel
+// with one method has half the code, and the voxel pipeline is large enough
+// for instruction fetch to show in its stalls.
 #ifndef DECAES_LEGACY_KERNEL
 #define DECAES_LEGACY_KERNEL 0
+#endif
+#ifndef DECAES_METHODS
+#define DECAES_METHODS 3
 #endif
 
 namespace dk {
 
 constexpr bool kLegacyKernel = DECAES_LEGACY_KERNEL != 0;
+constexpr bool kHasPlain = (DECAES_METHODS & 1) != 0, kHasMixed = (DECAES_METHODS & 2) != 0;
 
 struct Warp {
     const Params *P;
@@ -37,6 +45,9 @@ struct Warp {
     int ldA;
     bool mixed;    // the mixed method (Params::mixed)
 };
+// The warp's method, folded to a constant in single-method kernels.
+__device__ __forceinline__ bool use_mixed(const Warp &w) { return kHasMixed && (!kHasPlain || w.mixed); }
+
 
 __device__ __forceinline__ void note(Warp &w, const NnlsResult &r) { w.nnls_caps += (r.mode != 0); }
 
@@ -45,7 +56,7 @@ __device__ __forceinline__ void note(Warp &w, const NnlsResult &r) { w.nnls_caps
 // solver on the voxel's prepared Gram matrix for the mixed method.
 static __device__ NnlsResult basis_lsq(Warp &w, bool tikh, double mu) {
     const Params &P = *w.P;
-    if (w.mixed)
+    if (use_mixed(w))
         return gram_nnls(w.g, w.s.x, w.s.w, w.s.idx, P.n, tikh ? mu * mu : 0.0, 3 * P.n, &w.g.lastk);
     return warp_lsq(w.s, w.A, P.m, P.n, w.data, tikh, mu);
 }
@@ -505,7 +516,7 @@ static __device__ void lc_update_curvature(LCurve &L, const LcState &s, const do
     for (int q = 0; q < 4; ++q) {
         double x = s.x[q], P0 = s.P[2 * q], P1 = s.P[2 * q + 1];
         double C = -CUDART_INF;
-        const bool far = L.w->mixed ? fmin(sq2(P0 - Ptl[0], P1 - Ptl[1]), sq2(P0 - Pbr[0], P1 - Pbr[1])) > Ctol * Ctol
+        const bool far = use_mixed(*L.w) ? fmin(sq2(P0 - Ptl[0], P1 - Ptl[1]), sq2(P0 - Pbr[0], P1 - Pbr[1])) > Ctol * Ctol
                                     : jmin(nrm2(P0 - Ptl[0], P1 - Ptl[1]), nrm2(P0 - Pbr[0], P1 - Pbr[1])) > Ctol;
         if (far) {
             const long long kx = okey(x);
@@ -530,7 +541,7 @@ static __device__ void lc_update_curvature(LCurve &L, const LcState &s, const do
             double m0 = P0, m1 = P1, p0 = P0, p1 = P1;
             if (im >= 0) { m0 = L.pP[2 * im]; m1 = L.pP[2 * im + 1]; }
             if (ip >= 0) { p0 = L.pP[2 * ip]; p1 = L.pP[2 * ip + 1]; }
-            C = L.w->mixed ? menger_fast(m0, m1, P0, P1, p0, p1) : menger(m0, m1, P0, P1, p0, p1);
+            C = use_mixed(*L.w) ? menger_fast(m0, m1, P0, P1, p0, p1) : menger(m0, m1, P0, P1, p0, p1);
         }
         pc_set(L, x, P0, P1, C, false);
     }
@@ -588,7 +599,7 @@ static __device__ double lcurve_corner(LCurve &L, double xlow, double xhigh, dou
     double Ptl[2] = {st.P[0], st.P[1]}, Pbr[2] = {st.P[6], st.P[7]};
     lc_update_curvature(L, st, Ptl, Pbr, Ctol);
     int iter = 0;
-    const bool mixed = L.w->mixed;
+    const bool mixed = use_mixed(*L.w);
     while (!(fabs(st.x[3] - st.x[0]) < xtol || (mixed ? sq2(st.P[0] - st.P[6], st.P[1] - st.P[7]) < Ptol * Ptol
                                                       : nrm2(st.P[0] - st.P[6], st.P[1] - st.P[7]) < Ptol))) {
         iter += 1;
@@ -741,7 +752,7 @@ struct GcvF {  // log𝒢(logμ), src/lsqnonneg.jl:1150-1154 and gcv!, 1213-1229
         double res2 = tikh_res2(*w, t);
         int k = P.m < P.n ? P.m : P.n;
         double dof = (double)(P.m - P.n > 0 ? P.m - P.n : 0), l2 = mu * mu;
-        if (w->mixed) {  // lanes over singular values
+        if (use_mixed(*w)) {  // lanes over singular values
             double part = 0.0;
             #pragma unroll 1
             for (int i = w->lane; i < k; i += 32) { double g2 = gam[i] * gam[i]; part = fma(l2, fast_rcp(g2 + l2), part); }
@@ -757,7 +768,7 @@ struct GcvF {  // log𝒢(logμ), src/lsqnonneg.jl:1150-1154 and gcv!, 1213-1229
 static __device__ void reg_gcv(Warp &w, double &mu_out, double &chi2_out) {
     const Params &P = *w.P;
     double *gam = w.scr + (long)P.m * P.n + 3L * P.K + (long)kCacheCap * 19;
-    if (!w.mixed) warp_svdvals(w, gam);  // the mixed method takes them from its Gram matrix (gram_svdvals)
+    if (!use_mixed(w)) warp_svdvals(w, gam);  // the mixed method takes them from its Gram matrix (gram_svdvals)
     GcvF f{&w, gam, (2.220446049250313e-16 * 2.220446049250313e-16) / P.m};
     double logmu, logG;
     brent_minimize(f, -8.0, 2.0, 0.0, 1e-4, 20, logmu, logG);
@@ -797,7 +808,7 @@ static __device__ void fa_update(Search &S, int I) {
     const int m = P.m, n = P.n, lane = w.lane;
     const double *A = P.As + (long)(I - 1) * m * n, *dA = P.dAs + (long)(I - 1) * m * n;
     NnlsResult r;
-    if (w.mixed) {
+    if (use_mixed(w)) {
         // precomputed Gram matrix of grid basis I; A'b from its transposed copy
         gram_load(w.g, P.Gs + (long)(I - 1) * (n * (n + 1) / 2), n);
         gram_rhs_t(w.g, P.AsT + (long)(I - 1) * m * n, m, n, w.data);
@@ -1102,10 +1113,10 @@ static __device__ void process_voxel(Warp &w, long v) {
         } else {
             alpha = flip_angle_search(w);
         }
-        if (w.mixed) warp_basis_f32(w, alpha);
+        if (use_mixed(w)) warp_basis_f32(w, alpha);
         else warp_basis(w, alpha, w.A);
     }
-    if (w.mixed) {
+    if (use_mixed(w)) {
         // Gram matrix and right-hand side of the voxel's basis, shared by every
         // solve of the regularizer; GCV's singular values first (their
         // workspace overlaps the staged basis, not the Gram matrix)

@@ -15,7 +15,7 @@ static __device__ void warp_setup(Warp &w, const Params &P, double *p, double *s
     w.P = &P;
     w.mixed = P.mixed != 0;
     const int n = P.n, lda = P.lda;
-    if (w.mixed) {
+    if (use_mixed(w)) {
         // normal-equation workspace (see warp_smem_doubles_mixed)
         const int m = P.m;
         w.data = p; p += m;
