@@ -188,7 +188,7 @@ static __device__ __noinline__ void gram_load(GramWS &g, const double *Gg, int n
 // update spread over lanes by (row, column) pair, so a step costs ~(k-j)^2/64
 // FMA instructions instead of k-j.  Returns false when a pivot is not
 // positive relative to its diagonal (numerically dependent set).
-static __device__ bool gram_refactor(GramWS &g, int k, double mu2) {
+static __device__ __noinline__ bool gram_refactor(GramWS g, int k, double mu2) {
     const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;
     const int p0 = r0 < k ? g.P[r0] : 0, p1 = r1 < k ? g.P[r1] : 0;
@@ -255,7 +255,7 @@ static __device__ bool gram_refactor(GramWS &g, int k, double mu2) {
 // not positive relative to H_tt or when its coefficient y_t / delta in the
 // unconstrained solution on P + {t} is not positive (the guards of the
 // reference's Householder step).  Returns true when t was added.
-static __device__ bool gram_append(GramWS &g, int k, int t, double mu2) {
+static __device__ __noinline__ bool gram_append(GramWS g, int k, int t, double mu2) {
     const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;
     const double *L0 = g.L + tri(r0 - 1), *L1 = g.L + tri(r1 - 1);
@@ -291,7 +291,7 @@ static __device__ bool gram_append(GramWS &g, int k, int t, double mu2) {
 
 // z = L^{-T} D^{-1} y (unit upper back substitution, lanes over rows);
 // z returned in (z0, z1).
-static __device__ void gram_back(const GramWS &g, int k, double &z0, double &z1) {
+static __device__ __noinline__ double2 gram_back(const GramWS g, int k) {
     const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;
     double u0 = r0 < k ? g.y[r0] * g.dinv[r0] : 0.0, u1 = r1 < k ? g.y[r1] * g.dinv[r1] : 0.0;
@@ -302,8 +302,7 @@ static __device__ void gram_back(const GramWS &g, int k, double &z0, double &z1)
         if (r0 < i) u0 = fma(-Li[r0], zi, u0);
         if (r1 < i) u1 = fma(-Li[r1], zi, u1);
     }
-    z0 = u0;
-    z1 = u1;
+    return make_double2(u0, u1);
 }
 
 // Singular values of the basis for GCV, as square roots of the eigenvalues of
@@ -482,8 +481,8 @@ static __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double 
                 k = 0;
                 break;
             }
-            double z0, z1;
-            gram_back(g, k, z0, z1);
+            const double2 zz = gram_back(g, k);
+            const double z0 = zz.x, z1 = zz.y;
             const bool keep0 = r0 < k && z0 > 0, keep1 = r1 < k && z1 > 0;
             const unsigned m0 = __ballot_sync(FULL, keep0), m1 = __ballot_sync(FULL, keep1);
             const int kk = __popc(m0) + __popc(m1);
@@ -560,8 +559,8 @@ static __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double 
         // inner loop: move toward the unconstrained solution on P
         #pragma unroll 1
         for (;;) {
-            double z0, z1;
-            gram_back(g, k, z0, z1);
+            const double2 zz = gram_back(g, k);
+            const double z0 = zz.x, z1 = zz.y;
             const bool pos0 = !(r0 < k) || z0 > 0, pos1 = !(r1 < k) || z1 > 0;
             if (__all_sync(FULL, pos0 && pos1)) {
                 if (r0 < k) x[g.P[r0]] = z0;

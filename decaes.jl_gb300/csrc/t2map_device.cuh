@@ -28,6 +28,16 @@ namespace dk {
 constexpr bool kLegacyKernel = DECAES_LEGACY_KERNEL != 0;
 constexpr bool kHasPlain = (DECAES_METHODS & 1) != 0, kHasMixed = (DECAES_METHODS & 2) != 0;
 
+// Helpers with several call sites on the mixed method's hot path are kept out
+// of line in its single-method kernel (one copy in the instruction cache
+// instead of one per site: the kernel is ~0.5 MB of code and instruction
+// fetch is a visible stall); the other kernels inline them as before.
+#if DECAES_METHODS == 2
+#define DK_OUTLINE __noinline__
+#else
+#define DK_OUTLINE
+#endif
+
 struct Warp {
     const Params *P;
     NnlsWS s;
@@ -434,7 +444,7 @@ struct LCurve {
     bool overflow;
 };
 // f_lcurve(logμ) = (log ||Ax-b||^2, log ||x||^2) through the isapprox-keyed cache
-static __device__ void lc_eval(LCurve &L, double x, double &P0, double &P1) {
+static __device__ DK_OUTLINE void lc_eval(LCurve &L, double x, double &P0, double &P1) {
     int hit = warp_find_approx(L.fx, L.flen, x);
     if (hit >= 0) { P0 = L.fP[2 * hit]; P1 = L.fP[2 * hit + 1]; return; }
     Warp &w = *L.w;
@@ -453,7 +463,7 @@ static __device__ void lc_eval(LCurve &L, double x, double &P0, double &P1) {
     }
 }
 static __device__ int pc_find(const LCurve &L, double x) { return warp_find_approx(L.px, L.plen, x); }
-static __device__ void pc_set(LCurve &L, double x, double P0, double P1, double C, bool push_only) {
+static __device__ DK_OUTLINE void pc_set(LCurve &L, double x, double P0, double P1, double C, bool push_only) {
     int i = push_only ? -1 : pc_find(L, x);
     if (i < 0) {
         if (L.plen >= kCacheCap) { L.overflow = true; return; }
@@ -510,7 +520,7 @@ struct LcState {
 // update_curvature!, src/lsqnonneg.jl:948-965.  The nearest cached
 // neighbours (largest key below x, smallest above; first index on ties) are
 // found lanes-over-entries with integer keys.
-static __device__ void lc_update_curvature(LCurve &L, const LcState &s, const double *Ptl, const double *Pbr, double Ctol) {
+static __device__ DK_OUTLINE void lc_update_curvature(LCurve &L, const LcState &s, const double *Ptl, const double *Pbr, double Ctol) {
     const int lane = threadIdx.x & 31;
     #pragma unroll 1
     for (int q = 0; q < 4; ++q) {
@@ -852,7 +862,7 @@ static __device__ void fa_update(Search &S, int I) {
     S.npts++;
 }
 // update!(surr, state, I; maxeval), src/splines.jl:736-744
-static __device__ bool fa_state_update(Search &S, int I) {
+static __device__ DK_OUTLINE bool fa_state_update(Search &S, int I) {
     if (S.numeval >= S.maxeval) return true;
     if (sseen(S, I)) return false;
     fa_update(S, I);
@@ -942,7 +952,7 @@ static __device__ __noinline__ double2 fa_suggest_legacy(const double *angles, c
     }
     return make_double2(memo[1], memo[2]);
 }
-static __device__ void fa_suggest(Search &S, double &xo, double &uo) {
+static __device__ DK_OUTLINE void fa_suggest(Search &S, double &xo, double &uo) {
     const double *g = S.w->P->angles;
     if (kLegacyKernel && S.w->P->legacy) {
         double2 r = fa_suggest_legacy(g, S.u, S.sidx, S.npts, legacy_ws(*S.w));
