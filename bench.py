@@ -558,7 +558,7 @@ def main():
         if cv is not None:
             achieved = flops_per_voxel * Vp / (kern_ms * 1e-3) / 1e12
             tpv = profile_figure(f"k_voxels_fp64_{args.workload}.md", "dram_bytes_per_voxel")  # ncu on a small slab
-            line["roofline"] = {"kernel": "k_voxels (FP64 method)", "bound": "fp64", "achieved": achieved,
+            line["roofline"] = {"kernel": "k_voxels_plain (FP64 method)", "bound": "fp64", "achieved": achieved,
                                 "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                                 "traffic": None if tpv is None else tpv * Vp,
                                 "work": f"{flops_per_voxel / 1e6:.3f} MFLOP FP64 per above-threshold voxel "
@@ -570,7 +570,7 @@ def main():
         tpv = profile_figure(f"k_voxels_mixed_{args.workload}.md", "dram_bytes_per_voxel")
         if fpv is not None:
             achieved = fpv * Vp / (kern_ms * 1e-3) / 1e12
-            line["roofline"] = {"kernel": "k_voxels (mixed method)", "bound": "fp64", "achieved": achieved,
+            line["roofline"] = {"kernel": "k_voxels_mixed (mixed method)", "bound": "fp64", "achieved": achieved,
                                 "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                                 "traffic": None if tpv is None else tpv * Vp,
                                 "work": f"{fpv / 1e6:.3f} MFLOP FP64 per above-threshold voxel (executed by the "
