@@ -271,8 +271,8 @@ class _Null:
 
 def run_batch_workload(args):
     """The batched uneven workload: many volumes of different shapes solved by
-    one persistent launch (a prepared batch replayed as a CUDA graph), against
-    the same volumes solved one device call after another."""
+    one graph replay of a prepared batch (a persistent launch per occupancy
+    class), against the same volumes solved one device call after another."""
     import torch
     import decaes_gb300 as D
     from decaes_gb300 import _lib
@@ -334,7 +334,7 @@ def run_batch_workload(args):
     same = all(np.array_equal(np.nan_to_num(a, nan=-1), np.nan_to_num(sp[3]["sfr"].double().cpu().numpy(), nan=-1))
                for a, sp in zip(sfr_batch, specs))
     line = {
-        "metric": f"voxels/s, {nvol} uneven volumes in one persistent launch (prepared batch, CUDA graph replay)",
+        "metric": f"voxels/s, {nvol} uneven volumes in one graph replay (a persistent launch per occupancy class)",
         "value": V_tot / (ms * 1e-3), "unit": "voxels/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f64+f32",

@@ -135,9 +135,21 @@ __global__ void __launch_bounds__(128) k_voxels_batch(const __grid_constant__ Ba
 // the same kernels with the legacy algorithms (decaes_legacy.cu), and with one
 // method each (decaes_plain.cu, decaes_mixed.cu)
 __global__ void __launch_bounds__(128) k_voxels_legacy(const __grid_constant__ Params P);
+__global__ void __launch_bounds__(128) k_voxels_batch_legacy(const __grid_constant__ BatchParams B);
 __global__ void __launch_bounds__(128) k_voxels_plain(const __grid_constant__ Params P);
 __global__ void __launch_bounds__(128) k_voxels_mixed(const __grid_constant__ Params P);
-__global__ void __launch_bounds__(128) k_voxels_batch_legacy(const __grid_constant__ BatchParams B);
+__global__ void __launch_bounds__(128) k_voxels_batch_plain(const __grid_constant__ BatchParams B);
+__global__ void __launch_bounds__(128) k_voxels_batch_mixed(const __grid_constant__ BatchParams B);
+
+// The batched kernel for a set of volumes: the legacy one when any volume is
+// legacy, else the kernel of the volumes' one method, else the two-method one.
+using BatchKern = void (*)(BatchParams);
+inline BatchKern batch_kernel(bool legacy, bool any_plain, bool any_mixed) {
+    if (legacy) return k_voxels_batch_legacy;
+    if (!any_plain) return k_voxels_batch_mixed;
+    if (!any_mixed) return k_voxels_batch_plain;
+    return k_voxels_batch;
+}
 
 // offsets[0] = 0, offsets[v + 1] = offsets[v] + counts[v] (one thread; nvol is small).
 __global__ void k_batch_prefix(const int *counts, int nvol, int *offsets) {
@@ -863,6 +875,21 @@ struct BatchVol {
     double cost = 0;
     size_t out_off = 0, out_len = 0, vidx_off = 0, w_off = SIZE_MAX;
     OutMap om{};
+    long stride = 0, scr = 0;  // shared-memory doubles per warp (Params copy + workspace), global scratch doubles
+    int cls = 0;               // launch class
+};
+
+// One persistent launch of a batch: the volumes [first, first + count) of the
+// queue, with the workspace of its largest volume.  Volumes are grouped into
+// classes by the number of warps an SM can hold for them, so a small volume
+// never runs at the occupancy of the batch's largest one.
+struct BatchClass {
+    int first = 0, count = 0;
+    long smem_stride = 0, scr_stride = 0;
+    int wpb = 1, grid = 0;
+    size_t smem = 0;
+    double cost = 0;
+    dk::BatchKern kern = nullptr;
 };
 
 // Working memory and launch shape of a batch.  The buffers are the context's
@@ -879,11 +906,11 @@ struct BatchPrep {
     int *vidx = nullptr, *cnt = nullptr;  // cnt: counts[nvol], offsets[nvol + 1], counter
     unsigned long long *stats = nullptr;  // 2 per volume
     dk::Params *params = nullptr;
-    long smem_stride = 0, scr_stride = 0;
-    int wpb = 1, grid = 0;
-    size_t smem = 0;
-    bool legacy = false;  // some volume uses the legacy algorithms: the legacy kernel runs the batch
-    size_t cnt_bytes() const { return sizeof(int) * (2 * vols.size() + 2) + 16; }
+    std::vector<BatchClass> classes;  // launched one after another
+    long scr_doubles = 0;  // scratch of the largest class (classes run in sequence and share it)
+    // cnt: counts[nvol], then per class offsets[count + 1], then per class one queue counter
+    size_t cnt_ints() const { return 2 * vols.size() + 2 * classes.size(); }
+    size_t cnt_bytes() const { return sizeof(int) * cnt_ints() + 16; }
 };
 
 // Relative cost of a voxel: the autotuner's measurement, else a model of the
@@ -929,9 +956,38 @@ int batch_plan(decaes_ctx *ctx, const decaes_volume *vols, int nvol, cudaStream_
         bv.cost = voxel_cost(ctx, v.mopts) * (double)bv.V;
         bp.vols.push_back(bv);
     }
-    std::stable_sort(bp.vols.begin(), bp.vols.end(), [](const BatchVol &a, const BatchVol &b) { return a.cost > b.cost; });
+    // workspace of each volume and its occupancy class (warps per SM at its own workspace size)
+    for (BatchVol &bv : bp.vols) {
+        OutMap tmp;
+        layout_outputs(bv.v.mopts, bv.t2part, nullptr, tmp);
+        dk::Params P;
+        long wsm = 0;
+        if (int rc = make_params(ctx, bv.v.mopts, nullptr, nullptr, bv.B, nullptr, bv.v.dtype, nullptr, tmp, P, &wsm)) return rc;
+        bv.stride = ((long)dk::kParamsDoubles + wsm + 1) & ~1L;
+        bv.scr = P.scr_stride;
+        int wpb = 1, grid = 0;
+        size_t smem = 0;
+        if (int rc = launch_shape(ctx, dk::k_voxels_batch, bv.stride, &wpb, &grid, &smem)) return rc;
+        bv.cls = grid / std::max(ctx->sms, 1);  // warps per SM at wpb = 1
+    }
+    // classes in decreasing occupancy, each volume's queue position by cost
+    std::stable_sort(bp.vols.begin(), bp.vols.end(), [](const BatchVol &a, const BatchVol &b) {
+        return a.cls != b.cls ? a.cls > b.cls : a.cost > b.cost;
+    });
+    bp.classes.clear();
+    for (int q = 0; q < (int)bp.vols.size(); ++q) {
+        if (q == 0 || bp.vols[q].cls != bp.vols[q - 1].cls) {
+            BatchClass c;
+            c.first = q;
+            bp.classes.push_back(c);
+        }
+        BatchClass &c = bp.classes.back();
+        c.count++;
+        c.smem_stride = std::max(c.smem_stride, bp.vols[q].stride);
+        c.scr_stride = std::max(c.scr_stride, bp.vols[q].scr);
+        c.cost += bp.vols[q].cost;
+    }
     bp.n_out = bp.n_vidx = bp.n_w = 0;
-    bp.smem_stride = bp.scr_stride = 0;
     for (BatchVol &bv : bp.vols) {
         OutMap tmp;
         bv.out_len = layout_outputs(bv.v.mopts, bv.t2part, nullptr, tmp);
@@ -941,18 +997,21 @@ int batch_plan(decaes_ctx *ctx, const decaes_volume *vols, int nvol, cudaStream_
         bp.n_vidx += (size_t)std::max<long>(bv.V, 1);
         bv.w_off = SIZE_MAX;
         if (bv.t2part && !bv.pp.weights.empty()) { bv.w_off = bp.n_w; bp.n_w += bv.v.mopts.nT2; }
-        dk::Params P;
-        long wsm = 0;
-        if (int rc = make_params(ctx, bv.v.mopts, nullptr, nullptr, bv.B, nullptr, bv.v.dtype, nullptr, tmp, P, &wsm)) return rc;
-        bp.smem_stride = std::max(bp.smem_stride, (long)dk::kParamsDoubles + wsm);
-        bp.scr_stride = std::max(bp.scr_stride, P.scr_stride);
     }
-    bp.smem_stride = (bp.smem_stride + 1) & ~1L;
-    bp.legacy = false;
-    for (const BatchVol &bv : bp.vols) bp.legacy = bp.legacy || bv.v.mopts.legacy;
-    bp.wpb = tuned_wpb(ctx, bp.vols[0].v.mopts);
-    return launch_shape(ctx, bp.legacy ? dk::k_voxels_batch_legacy : dk::k_voxels_batch, bp.smem_stride, &bp.wpb,
-                        &bp.grid, &bp.smem);
+    bp.scr_doubles = 0;
+    for (BatchClass &c : bp.classes) {
+        bool legacy = false, any_plain = false, any_mixed = false;
+        for (int q = c.first; q < c.first + c.count; ++q) {
+            const decaes_t2map_opts &o = bp.vols[q].v.mopts;
+            legacy = legacy || o.legacy;
+            (o.precision == DECAES_PREC_MIXED ? any_mixed : any_plain) = true;
+        }
+        c.kern = dk::batch_kernel(legacy, any_plain, any_mixed);
+        c.wpb = tuned_wpb(ctx, bp.vols[c.first].v.mopts);
+        if (int rc = launch_shape(ctx, c.kern, c.smem_stride, &c.wpb, &c.grid, &c.smem)) return rc;
+        bp.scr_doubles = std::max(bp.scr_doubles, c.scr_stride * c.grid * c.wpb);
+    }
+    return DECAES_OK;
 }
 
 size_t batch_bytes(const BatchPrep &bp, size_t *b_out, size_t *b_vidx, size_t *b_w, size_t *b_par, size_t *b_scr) {
@@ -960,7 +1019,7 @@ size_t batch_bytes(const BatchPrep &bp, size_t *b_out, size_t *b_vidx, size_t *b
     *b_vidx = sizeof(int) * std::max<size_t>(bp.n_vidx, 1);
     *b_w = sizeof(double) * std::max<size_t>(bp.n_w, 1);
     *b_par = sizeof(dk::Params) * bp.vols.size() + bp.cnt_bytes() + 16 * bp.vols.size();
-    *b_scr = sizeof(double) * (size_t)bp.scr_stride * bp.grid * bp.wpb;
+    *b_scr = sizeof(double) * (size_t)std::max<long>(bp.scr_doubles, 1);
     return *b_out + *b_vidx + *b_w + *b_par + *b_scr;
 }
 
@@ -997,8 +1056,8 @@ int batch_bind(decaes_ctx *ctx, BatchPrep &bp, void *outs, void *vidx, void *w, 
 // The batch's launch sequence on st: memsets, kernels and device copies only,
 // so it can be captured into a CUDA graph.
 int batch_enqueue(decaes_ctx *ctx, const BatchPrep &bp, cudaStream_t st, int *launches) {
-    const int nvol = (int)bp.vols.size();
-    int *counts = bp.cnt, *offsets = bp.cnt + nvol, *counter = bp.cnt + 2 * nvol + 1;
+    const int nvol = (int)bp.vols.size(), ncls = (int)bp.classes.size();
+    int *counts = bp.cnt, *offsets = bp.cnt + nvol, *counters = offsets + nvol + ncls;
     CK(cudaMemsetAsync(bp.cnt, 0, bp.cnt_bytes(), st));
     CK(cudaMemsetAsync(bp.stats, 0, 16 * nvol, st));
     for (int q = 0; q < nvol; ++q) {
@@ -1010,10 +1069,15 @@ int batch_enqueue(decaes_ctx *ctx, const BatchPrep &bp, cudaStream_t st, int *la
                                                       bp.vidx + bv.vidx_off, counts + q);
         *launches += 2;
     }
-    dk::k_batch_prefix<<<1, 32, 0, st>>>(counts, nvol, offsets);
-    dk::BatchParams B{bp.params, offsets, nvol, counter, bp.scratch, bp.scr_stride, bp.smem_stride};
-    (bp.legacy ? dk::k_voxels_batch_legacy : dk::k_voxels_batch)<<<bp.grid, 32 * bp.wpb, bp.smem, st>>>(B);
-    *launches += 2;
+    // one persistent launch per occupancy class, in sequence (they share the scratch)
+    for (int c = 0; c < ncls; ++c) {
+        const BatchClass &k = bp.classes[c];
+        int *off = offsets + k.first + c;  // this class's count + 1 offsets
+        dk::k_batch_prefix<<<1, 32, 0, st>>>(counts + k.first, k.count, off);
+        dk::BatchParams B{bp.params + k.first, off, k.count, counters + c, bp.scratch, k.scr_stride, k.smem_stride};
+        k.kern<<<k.grid, 32 * k.wpb, k.smem, st>>>(B);
+        *launches += 2;
+    }
     for (int q = 0; q < nvol; ++q) {
         const BatchVol &bv = bp.vols[q];
         const decaes_t2map_out &d = bv.v.d_mout;
@@ -1468,9 +1532,12 @@ std::vector<Chunk> srv_launch_tick(decaes_server *S) {
     smem_stride = (smem_stride + 1) & ~1L;
     int wpb = 1, grid = 0;
     size_t smem = 0;
-    bool legacy = false;
-    for (int q = 0; q < nq; ++q) legacy = legacy || ch[q].r->mo.legacy;
-    auto kern = legacy ? dk::k_voxels_batch_legacy : dk::k_voxels_batch;
+    bool legacy = false, any_plain = false, any_mixed = false;
+    for (int q = 0; q < nq; ++q) {
+        legacy = legacy || ch[q].r->mo.legacy;
+        (ch[q].r->mo.precision == DECAES_PREC_MIXED ? any_mixed : any_plain) = true;
+    }
+    const dk::BatchKern kern = dk::batch_kernel(legacy, any_plain, any_mixed);
     if (ok) {
         wpb = tuned_wpb(ctx, ch[0].r->mo);
         ok = launch_shape(ctx, kern, smem_stride, &wpb, &grid, &smem) == DECAES_OK;

@@ -1,6 +1,6 @@
 // decaes_mixed.cu -- the voxel-solve kernel with the mixed-precision method only: single-volume launches
-// of that method use it (half the code of the kernel that carries both
-// methods, which the batched and served launches keep).  A separate
+// and batched / served launches whose volumes all use that method run these
+// kernels (half the code of the kernels that carry both methods).  A separate
 // translation unit, compiled in parallel with the others.
 #define DECAES_METHODS 2
 #include "voxel_kernels.cuh"
@@ -8,5 +8,6 @@
 namespace dk {
 
 __global__ void __launch_bounds__(128) k_voxels_mixed(const __grid_constant__ Params P) { voxels_body(P); }
+__global__ void __launch_bounds__(128) k_voxels_batch_mixed(const __grid_constant__ BatchParams B) { voxels_batch_body(B); }
 
 }  // namespace dk
