@@ -1513,10 +1513,38 @@ std::vector<Chunk> srv_launch_tick(decaes_server *S) {
         r->inflight++;
     }
     if (ch.empty()) return ch;
-    std::stable_sort(ch.begin(), ch.end(), [](const Chunk &a, const Chunk &b) { return a.cost > b.cost; });
+    // each chunk's workspace and occupancy class (as for batches: one
+    // persistent launch per class, so small shapes keep their occupancy)
     const int nq = (int)ch.size();
-    long smem_stride = 0, scr_stride = 0, voff = 0;
+    std::vector<long> stride(nq), scr(nq);
+    std::vector<int> cls(nq);
     bool ok = true;
+    for (int q = 0; q < nq && ok; ++q) {
+        dk::Params P;
+        long wsm = 0;
+        ok = make_params(ctx, ch[q].r->mo, nullptr, nullptr, ch[q].r->B, nullptr, ch[q].r->dtype, nullptr, ch[q].r->om, P,
+                         &wsm) == DECAES_OK;
+        stride[q] = ((long)dk::kParamsDoubles + wsm + 1) & ~1L;
+        scr[q] = P.scr_stride;
+        int wpb = 1, grid = 0;
+        size_t smem = 0;
+        ok = ok && launch_shape(ctx, dk::k_voxels_batch, stride[q], &wpb, &grid, &smem) == DECAES_OK;
+        cls[q] = grid / std::max(ctx->sms, 1);
+    }
+    std::vector<int> order(nq);
+    for (int q = 0; q < nq; ++q) order[q] = q;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return cls[a] != cls[b] ? cls[a] > cls[b] : ch[a].cost > ch[b].cost;
+    });
+    {
+        std::vector<Chunk> c2;
+        std::vector<long> s2, r2;
+        std::vector<int> k2;
+        for (int q : order) { c2.push_back(ch[q]); s2.push_back(stride[q]); r2.push_back(scr[q]); k2.push_back(cls[q]); }
+        ch.swap(c2); stride.swap(s2); scr.swap(r2); cls.swap(k2);
+    }
+    std::vector<BatchClass> classes;
+    long voff = 0;
     for (int q = 0; q < nq && ok; ++q) {
         const Chunk &c = ch[q];
         long wsm = 0;
@@ -1526,23 +1554,30 @@ std::vector<Chunk> srv_launch_tick(decaes_server *S) {
         S->h_params[q].nvox = S->d_cnt + q;
         S->h_params[q].stats = S->d_stats + 2 * q;
         voff += c.v1 - c.v0;
-        smem_stride = std::max(smem_stride, (long)dk::kParamsDoubles + wsm);
-        scr_stride = std::max(scr_stride, S->h_params[q].scr_stride);
+        if (q == 0 || cls[q] != cls[q - 1]) {
+            BatchClass k;
+            k.first = q;
+            classes.push_back(k);
+        }
+        BatchClass &k = classes.back();
+        k.count++;
+        k.smem_stride = std::max(k.smem_stride, stride[q]);
+        k.scr_stride = std::max(k.scr_stride, scr[q]);
     }
-    smem_stride = (smem_stride + 1) & ~1L;
-    int wpb = 1, grid = 0;
-    size_t smem = 0;
-    bool legacy = false, any_plain = false, any_mixed = false;
-    for (int q = 0; q < nq; ++q) {
-        legacy = legacy || ch[q].r->mo.legacy;
-        (ch[q].r->mo.precision == DECAES_PREC_MIXED ? any_mixed : any_plain) = true;
+    long scr_doubles = 0;
+    for (BatchClass &k : classes) {
+        if (!ok) break;
+        bool legacy = false, any_plain = false, any_mixed = false;
+        for (int q = k.first; q < k.first + k.count; ++q) {
+            legacy = legacy || ch[q].r->mo.legacy;
+            (ch[q].r->mo.precision == DECAES_PREC_MIXED ? any_mixed : any_plain) = true;
+        }
+        k.kern = dk::batch_kernel(legacy, any_plain, any_mixed);
+        k.wpb = tuned_wpb(ctx, ch[k.first].r->mo);
+        ok = launch_shape(ctx, k.kern, k.smem_stride, &k.wpb, &k.grid, &k.smem) == DECAES_OK;
+        scr_doubles = std::max(scr_doubles, k.scr_stride * k.grid * k.wpb);
     }
-    const dk::BatchKern kern = dk::batch_kernel(legacy, any_plain, any_mixed);
-    if (ok) {
-        wpb = tuned_wpb(ctx, ch[0].r->mo);
-        ok = launch_shape(ctx, kern, smem_stride, &wpb, &grid, &smem) == DECAES_OK;
-    }
-    const size_t need = sizeof(double) * (size_t)scr_stride * grid * wpb;
+    const size_t need = sizeof(double) * (size_t)scr_doubles;
     if (ok && need > S->scratch_bytes) {
         if (S->d_scratch) cudaFreeAsync(S->d_scratch, S->comp);
         S->d_scratch = nullptr;
@@ -1550,9 +1585,10 @@ std::vector<Chunk> srv_launch_tick(decaes_server *S) {
         S->scratch_bytes = ok ? need : 0;
     }
     cudaStream_t st = S->comp;
-    int *counts = S->d_cnt, *offsets = S->d_cnt + nq, *counter = S->d_cnt + 2 * nq + 1;
+    const int ncls = (int)classes.size();
+    int *counts = S->d_cnt, *offsets = S->d_cnt + nq, *counters = offsets + nq + ncls;
     if (ok) ok = cudaMemcpyAsync(S->d_params, S->h_params, sizeof(dk::Params) * nq, cudaMemcpyHostToDevice, st) == cudaSuccess &&
-                 cudaMemsetAsync(S->d_cnt, 0, sizeof(int) * (2 * nq + 2), st) == cudaSuccess &&
+                 cudaMemsetAsync(S->d_cnt, 0, sizeof(int) * (2 * nq + 2 * ncls), st) == cudaSuccess &&
                  cudaMemsetAsync(S->d_stats, 0, 16 * nq, st) == cudaSuccess;
     if (ok) {
         cudaEventRecord(S->tick_t0, st);
@@ -1565,9 +1601,13 @@ std::vector<Chunk> srv_launch_tick(decaes_server *S) {
                                                                 c.r->mo.Threshold, S->d_vidx + vo, counts + q);
             vo += c.v1 - c.v0;
         }
-        dk::k_batch_prefix<<<1, 32, 0, st>>>(counts, nq, offsets);
-        dk::BatchParams B{S->d_params, offsets, nq, counter, S->d_scratch, scr_stride, smem_stride};
-        kern<<<grid, 32 * wpb, smem, st>>>(B);
+        for (int c = 0; c < ncls; ++c) {
+            const BatchClass &k = classes[c];
+            int *off = offsets + k.first + c;
+            dk::k_batch_prefix<<<1, 32, 0, st>>>(counts + k.first, k.count, off);
+            dk::BatchParams B{S->d_params + k.first, off, k.count, counters + c, S->d_scratch, k.scr_stride, k.smem_stride};
+            k.kern<<<k.grid, 32 * k.wpb, k.smem, st>>>(B);
+        }
         ok = cudaGetLastError() == cudaSuccess && cudaEventRecord(S->tick_t1, st) == cudaSuccess;
     }
     if (!ok) {
@@ -1629,7 +1669,7 @@ extern "C" decaes_server *decaes_server_create(decaes_ctx *ctx, const decaes_ser
               cudaEventCreate(&S->tick_t0) == cudaSuccess && cudaEventCreate(&S->tick_t1) == cudaSuccess &&
               cudaMalloc(&S->d_params, sizeof(dk::Params) * S->cap_chunks) == cudaSuccess &&
               cudaMallocHost(&S->h_params, sizeof(dk::Params) * S->cap_chunks) == cudaSuccess &&
-              cudaMalloc(&S->d_cnt, sizeof(int) * (2 * S->cap_chunks + 2)) == cudaSuccess &&
+              cudaMalloc(&S->d_cnt, sizeof(int) * (4 * S->cap_chunks + 2)) == cudaSuccess &&
               cudaMalloc(&S->d_stats, 16 * S->cap_chunks) == cudaSuccess &&
               cudaMalloc(&S->d_vidx, sizeof(int) * (size_t)S->tick_voxels) == cudaSuccess;
     if (!ok) {
