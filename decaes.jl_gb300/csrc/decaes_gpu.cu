@@ -369,10 +369,10 @@ struct OutMap {  // device double buffers for each output
 // Gram matrices, made on first use).
 int prepare_basis(decaes_ctx *ctx, const decaes_t2map_opts &o, cudaStream_t st, Basis **out, int *launches) {
     const int m = o.nTE, n = o.nT2;
-    if (m > 128) return fail(ctx, DECAES_EINVAL, "nTE > 128 is not supported by this build");
-    if (n > 256) return fail(ctx, DECAES_EINVAL, "nT2 > 256 is not supported by this build");
+    if (m > 128) return fail(ctx, DECAES_EINVAL, "nTE > 128 is not supported by libdecaes_gpu");
+    if (n > 256) return fail(ctx, DECAES_EINVAL, "nT2 > 256 is not supported by libdecaes_gpu");
     const bool fixed = !std::isnan(o.SetFlipAngle);
-    if (!fixed && o.nRefAngles > 256) return fail(ctx, DECAES_EINVAL, "nRefAngles > 256 is not supported by this build");
+    if (!fixed && o.nRefAngles > 256) return fail(ctx, DECAES_EINVAL, "nRefAngles > 256 is not supported by libdecaes_gpu");
     const bool mixed = o.precision == DECAES_PREC_MIXED;
     if (mixed && n > dk::kGramMaxN)
         return fail(ctx, DECAES_EINVAL, "precision = mixed supports nT2 <= " + std::to_string(dk::kGramMaxN));

@@ -149,9 +149,9 @@ extern "C" int decaes_t2map_t2part_noalloc(const decaes_t2map_opts *mopts, const
     const bool fixed = !std::isnan(o.SetFlipAngle);
     const int K = fixed ? 1 : o.nRefAngles;
     const long V = (long)o.MatrixSize[0] * o.MatrixSize[1] * o.MatrixSize[2];
-    if (m > 128) return fail(err, errlen, DECAES_EINVAL, "nTE > 128 is not supported by this build");
-    if (n > 256) return fail(err, errlen, DECAES_EINVAL, "nT2 > 256 is not supported by this build");
-    if (K > 256) return fail(err, errlen, DECAES_EINVAL, "nRefAngles > 256 is not supported by this build");
+    if (m > 128) return fail(err, errlen, DECAES_EINVAL, "nTE > 128 is not supported by libdecaes_gpu");
+    if (n > 256) return fail(err, errlen, DECAES_EINVAL, "nT2 > 256 is not supported by libdecaes_gpu");
+    if (K > 256) return fail(err, errlen, DECAES_EINVAL, "nRefAngles > 256 is not supported by libdecaes_gpu");
 
     int dev = 0;
     NA_CK(cudaGetDevice(&dev));

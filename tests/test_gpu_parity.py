@@ -14,11 +14,11 @@ pytestmark = pytest.mark.gpu
 SPWIN, MPWIN = (10e-3, 25e-3), (25e-3, 200e-3)
 
 CASES = {
-    # configs[0]: 32 echoes, chi2 1.02, 8 angles over 50-180 (sized down in voxels)
+    # 32 echoes, chi2 1.02, 8 angles over 50-180 (the reference's small CPU case, sized down in voxels)
     "chi2": dict(X=(8, 8, 2), m=32, TE=10e-3, n=40, T2=(10e-3, 2.0), K=8, Reg="chi2", Chi2Factor=1.02),
-    # configs[1]: 48 echoes, 32 angles, lcurve, 35% background below threshold
+    # 48 echoes, 32 angles, lcurve, 35% background below threshold (the 240x240x48 volume's settings)
     "lcurve": dict(X=(8, 8, 2), m=48, TE=10e-3, n=40, T2=(10e-3, 2.0), K=32, Reg="lcurve", bg=0.35, thr=200.0),
-    # configs[2] shapes: 56 echoes, TE 7 ms, 60 T2s over 8 ms-2 s, 64 angles, gcv
+    # 56 echoes, TE 7 ms, 60 T2s over 8 ms-2 s, 64 angles, gcv (the 240x240x113 volume's settings)
     "gcv": dict(X=(4, 4, 1), m=56, TE=7e-3, n=60, T2=(8e-3, 2.0), K=64, Reg="gcv"),
     "none": dict(X=(6, 6, 1), m=48, TE=10e-3, n=40, T2=(10e-3, 2.0), K=16, Reg="none"),
     "mdp": dict(X=(6, 6, 1), m=48, TE=10e-3, n=40, T2=(10e-3, 2.0), K=16, Reg="mdp", NoiseLevel=2.0),
