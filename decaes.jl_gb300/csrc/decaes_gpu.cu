@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(128) k_voxels_batch(const __grid_constant__ Ba
 // method each (decaes_plain.cu, decaes_mixed.cu)
 __global__ void __launch_bounds__(128) k_voxels_legacy(const __grid_constant__ Params P);
 __global__ void __launch_bounds__(128) k_voxels_batch_legacy(const __grid_constant__ BatchParams B);
-__global__ void __launch_bounds__(128) k_voxels_plain(const __grid_constant__ Params P);
+__global__ void __launch_bounds__(256) k_voxels_plain(const __grid_constant__ Params P);
 __global__ void __launch_bounds__(128) k_voxels_mixed(const __grid_constant__ Params P);
 __global__ void __launch_bounds__(128) k_voxels_batch_plain(const __grid_constant__ BatchParams B);
 __global__ void __launch_bounds__(128) k_voxels_batch_mixed(const __grid_constant__ BatchParams B);
@@ -439,13 +439,37 @@ int make_params(decaes_ctx *ctx, const decaes_t2map_opts &o, const dh::T2partPla
 }
 
 // Warps per block of the voxel kernel for a problem shape (autotuned, else 1).
-int tuned_wpb(decaes_ctx *ctx, const decaes_t2map_opts &o) {
+// Warps per block for a launch of these options: forced, else autotuned,
+// else 0 (no preference).
+int tuned_wpb_or0(decaes_ctx *ctx, const decaes_t2map_opts &o) {
     if (ctx->force_wpb) return ctx->force_wpb;
     const bool fixed = !std::isnan(o.SetFlipAngle);
     TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, o.precision == DECAES_PREC_MIXED, o.RefConAngle == 180.0,
               o.legacy != 0};
     auto it = ctx->tune.find(k);
-    return it == ctx->tune.end() ? 1 : it->second.wpb;
+    return it == ctx->tune.end() ? 0 : it->second.wpb;
+}
+int tuned_wpb(decaes_ctx *ctx, const decaes_t2map_opts &o) {
+    const int w = tuned_wpb_or0(ctx, o);
+    return w > 0 ? w : 1;
+}
+
+// The block size (1..max_wpb warps) that keeps the most warps resident per SM
+// for a kernel whose warps each need `stride` doubles of shared memory (each
+// block also reserves shared memory of its own, so one large block can hold a
+// warp more than single-warp blocks do); ties go to the smaller block.
+template <class Kern>
+int most_warps_wpb(decaes_ctx *ctx, Kern kern, long stride, int max_wpb) {
+    int best = 1, best_warps = 0;
+    for (int w = 1; w <= max_wpb; ++w) {
+        const size_t smem = (size_t)w * stride * sizeof(double);
+        if (smem > ctx->smem_optin) break;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) break;
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * w, smem) != cudaSuccess) break;
+        if (per_sm * w > best_warps) { best_warps = per_sm * w; best = w; }
+    }
+    return best;
 }
 
 // Persistent grid for a kernel whose warps each need `stride` doubles of
@@ -514,6 +538,9 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
     int wpb = tuned_wpb(ctx, o), grid = 0;
     size_t smem = 0;
     auto kern = o.legacy ? dk::k_voxels_legacy : (o.precision == DECAES_PREC_MIXED ? dk::k_voxels_mixed : dk::k_voxels_plain);
+    // the plain method's large workspace: blocks of up to 8 warps can hold a
+    // warp per SM more than single-warp blocks (its kernel allows 256 threads)
+    if (kern == dk::k_voxels_plain && tuned_wpb_or0(ctx, o) == 0) wpb = most_warps_wpb(ctx, kern, wsm, 8);
     if (int rc = launch_shape(ctx, kern, wsm, &wpb, &grid, &smem)) return rc;
     void *scr;
     if (int rc = buf(ctx, "scratch", sizeof(double) * (size_t)P.scr_stride * grid * wpb, &scr)) return rc;

@@ -37,7 +37,7 @@ __global__ void k_basis_fixed(int m, int n, double alpha, double TE, double T1, 
                               const double *t2, double *A, double *work);
 __global__ void k_fill(double *p, long len, double v);
 __global__ void k_compact(const void *image, int f32, long V, double thr, int *vidx, int *nvox);
-__global__ void __launch_bounds__(128) k_voxels_plain(const __grid_constant__ Params P);
+__global__ void __launch_bounds__(256) k_voxels_plain(const __grid_constant__ Params P);
 __global__ void __launch_bounds__(128) k_voxels_legacy(const __grid_constant__ Params P);
 }  // namespace dk
 

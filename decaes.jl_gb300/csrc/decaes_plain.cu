@@ -7,7 +7,7 @@
 
 namespace dk {
 
-__global__ void __launch_bounds__(128) k_voxels_plain(const __grid_constant__ Params P) { voxels_body(P); }
+__global__ void __launch_bounds__(256) k_voxels_plain(const __grid_constant__ Params P) { voxels_body(P); }
 __global__ void __launch_bounds__(128) k_voxels_batch_plain(const __grid_constant__ BatchParams B) { voxels_batch_body(B); }
 
 }  // namespace dk
