@@ -45,3 +45,35 @@ def test_cli_b1map(D, ctx, tmp_path):
                   "--Reg", "none", "--B1map", str(tmp_path / "b1.nii"), "--quiet"], ctx=ctx)
     m = io.loadmat(str(tmp_path / "mese.t2maps.mat"))
     np.testing.assert_array_equal(m["alpha"], b1)
+
+
+def test_daemon_on_gpu(D, ctx, tmp_path, monkeypatch):
+    """The warm daemon serves two command lines with one context; results
+    equal the direct API call's."""
+    import socket
+    import threading
+    io = pytest.importorskip("scipy.io")
+    from decaes_gb300 import daemon, nifti
+    X = (5, 4, 2)
+    img = D.mock_image(D.MockImageOptions(MatrixSize=X, nTE=32, TE=10e-3), seed=12)
+    nifti.write(str(tmp_path / "a.nii"), img)
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    srv = daemon.make_server(port, ctx=ctx)
+    th = threading.Thread(target=srv.serve_forever, daemon=True)
+    th.start()
+    try:
+        monkeypatch.chdir(tmp_path)
+        args = ["a.nii", "--T2map", "--TE", "10e-3", "--nT2", "40", "--T2Range", "10e-3", "2.0", "--Reg", "chi2",
+                "--RegParams", "1.02", "--quiet"]
+        assert daemon.run(args + ["-o", "r1"], port) == 0
+        assert daemon.run(args + ["-o", "r2", "--precision", "mixed"], port) == 0
+    finally:
+        srv.shutdown()
+        srv.server_close()
+    mo = D.T2mapOptions(MatrixSize=X, nTE=32, TE=10e-3, nT2=40, T2Range=(10e-3, 2.0), Reg="chi2", Chi2Factor=1.02)
+    maps, dist = D.T2mapSEcorr(np.asfortranarray(img, dtype=np.float64), mo, ctx=ctx)
+    np.testing.assert_array_equal(io.loadmat(str(tmp_path / "r1" / "a.t2dist.mat"))["dist"], dist)
+    assert (tmp_path / "r2" / "a.t2maps.mat").exists()
