@@ -577,7 +577,27 @@ def main():
                                         f"mixed method, ncu thread-instruction counts, FMA = 2) x {Vp} voxels",
                                 "kernel_ms": kern_ms,
                                 "peak_source": "cuBLAS DGEMM (torch.matmul float64 4096^3) measured in this run"}
+    if "roofline" in line:
+        line["roofline"]["hbm_view"] = hbm_view(mo, Vp, V, kern_ms)
     print(json.dumps(line), flush=True)
+
+
+def hbm_view(mo, Vp, V, kern_ms):
+    """The same kernel against HBM: the bytes it must move (the FP32 echo
+    train of every voxel for the threshold test and of each processed voxel
+    for its solve, its FP64 distribution, six maps and four T2 parts) over the
+    launch time, against the measured HBM copy bandwidth.  It shows how far
+    from HBM-bound the path is; the FP64 view above is the binding one."""
+    bytes_ = 4.0 * V + 4.0 * mo.nTE * Vp + 8.0 * (mo.nT2 + 10) * Vp
+    achieved = bytes_ / (kern_ms * 1e-3) / 1e9
+    peak, src = None, None
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            peak, src = float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"
+    except (OSError, ValueError, KeyError):
+        peak, src = 6800.0, "fallback 6.8 TB/s"
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "algorithmic_bytes_per_step": bytes_, "peak_source": src}
 
 
 if __name__ == "__main__":
