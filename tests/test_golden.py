@@ -1,0 +1,61 @@
+"""Committed regression fixtures (tests/golden/, made by make_golden.py from
+the oracle on small seeded inputs; the Julia reference cannot run here):
+the oracle reproduces them bit for bit on the CPU, and the CUDA path (FP64
+method) reproduces them on the GPU within the stated tolerances (bitwise in
+practice)."""
+import glob
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import make_golden as G  # noqa: E402
+
+NAMES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "golden", "*.npz")))
+
+
+def load(name):
+    with np.load(os.path.join(HERE, "golden", name + ".npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
+def test_fixtures_present():
+    assert set(NAMES) == set(G.CASES)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_reproduces_fixture(orc, name):
+    f = load(name)
+    mo, po = G.options(orc, name)
+    maps, dist = orc.t2map(f["image"], mo, nthreads=2)
+    parts = orc.t2part(dist, po)
+    np.testing.assert_array_equal(dist, f["dist"])
+    for k, v in maps.items():
+        np.testing.assert_array_equal(v, f["map_" + k], err_msg=k)
+    for k, v in parts.items():
+        np.testing.assert_array_equal(v, f["part_" + k], err_msg=k)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", NAMES)
+def test_gpu_reproduces_fixture(D, ctx, name):
+    f = load(name)
+    X, m, TE, n, T2, reg, K, extra = G.CASES[name]
+    kw = dict(MatrixSize=X, nTE=m, TE=TE, nT2=n, T2Range=T2, Reg=reg, nRefAngles=K, SaveRegParam=True,
+              SaveResidualNorm=True)
+    kw.update(extra)
+    o = D.T2mapOptions(**kw)
+    po = D.T2partOptions.from_t2map(o, SPWin=G.SPWIN, MPWin=G.MPWIN)
+    maps, dist, parts = D.T2mapSEcorr_T2partSEcorr(np.asfortranarray(f["image"]), o, po, ctx=ctx)
+    ref = f["dist"]
+    np.testing.assert_array_equal(np.isnan(dist), np.isnan(ref))
+    ok = ~np.isnan(ref)
+    scale = np.maximum(np.abs(ref), 1e-12 * np.nansum(np.abs(ref), axis=-1, keepdims=True))
+    assert np.all(np.abs(dist - ref)[ok] <= 1e-8 * scale[ok])
+    assert np.nanmax(np.abs(parts["sfr"] - f["part_sfr"])) <= 1e-10
+    for k in ("alpha", "mu", "chi2factor", "gdn", "ggm", "resnorm"):
+        np.testing.assert_allclose(maps[k], f["map_" + k], rtol=1e-8, atol=0, equal_nan=True, err_msg=k)
+    print(f"{name}: dist bitwise {np.array_equal(dist, ref)}")
