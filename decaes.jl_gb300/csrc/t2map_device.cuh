@@ -51,7 +51,6 @@ struct Warp {
     unsigned nnls_caps, loop_caps;
     // mixed method: normal-equation workspace and the staged basis (shared)
     GramWS g;
-    const float *Af;  // mixed method: the voxel's FP32 basis (column-major m x n, global scratch), else null
     float *As32;   // FP32 basis staged in shared memory, column-major, leading dimension ldA
     int ldA;
     bool mixed;    // the mixed method (Params::mixed)
@@ -1048,10 +1047,10 @@ static __device__ void warp_basis(Warp &w, double alpha, double *out /* m x n, g
 
 // Mixed method: the same curves with the recursion in FP32 (coefficients in
 // FP64, rounded once), states in the Gram and factor regions, curves written
-// as FP32 to the warp's global scratch (w.Af) and staged in w.As32.  The basis
-// of the voxel is these FP32 values, for the Gram matrix and the fitted curve
-// alike (the fit widens them exactly, on the integer pipes, so no FP32 <->
-// FP64 conversion occupies the FP64 pipe and no FP64 copy is written).
+// as FP32 to the warp's global scratch, then staged in w.As32 and widened
+// (exactly, on the integer pipes) into w.A.  The basis of the voxel is these
+// FP32 values, for the Gram matrix and the fitted curve alike, and no FP32 <->
+// FP64 conversion occupies the FP64 pipe.
 static __device__ void warp_basis_f32(Warp &w, double alpha) {
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lanes = P.epg_lanes_f32, lane = w.lane;
@@ -1077,7 +1076,9 @@ static __device__ void warp_basis_f32(Warp &w, double alpha) {
     #pragma unroll 1
     for (long q = lane; q < (long)m * n; q += 32) {
         const int i = (int)(q % m), j = (int)(q / m);
-        w.As32[i + w.ldA * j] = Af[q];
+        const float v = Af[q];
+        w.A[q] = widen(v);
+        w.As32[i + w.ldA * j] = v;
     }
     __threadfence_block();
     __syncwarp();
@@ -1112,7 +1113,6 @@ static __device__ void process_voxel(Warp &w, long v) {
 
     double alpha;
     w.g.lastk = 0;  // warm starts never cross voxels (results independent of scheduling)
-    w.Af = nullptr;
     if (P.angle_mode == 1) {
         alpha = P.fixed_angle;
         w.A = const_cast<double *>(P.basis_fixed);
@@ -1123,12 +1123,8 @@ static __device__ void process_voxel(Warp &w, long v) {
         } else {
             alpha = flip_angle_search(w);
         }
-        if (use_mixed(w)) {
-            warp_basis_f32(w, alpha);
-            w.Af = reinterpret_cast<const float *>(w.scr + warp_scratch_f32_offset(m, n, P.K));
-        } else {
-            warp_basis(w, alpha, w.A);
-        }
+        if (use_mixed(w)) warp_basis_f32(w, alpha);
+        else warp_basis(w, alpha, w.A);
     }
     if (use_mixed(w)) {
         // Gram matrix and right-hand side of the voxel's basis, shared by every
@@ -1178,13 +1174,8 @@ static __device__ void process_voxel(Warp &w, long v) {
         int i = lane + 32 * t;
         if (i < m) {
             double fit = 0;
-            if (use_mixed(w) && w.Af) {
-                #pragma unroll 1
-                for (int j = 0; j < n; ++j) fit = fma(widen(w.Af[i + (long)j * m]), w.s.w[j], fit);
-            } else {
-                #pragma unroll 1
-                for (int j = 0; j < n; ++j) fit = fma(w.A[i + (long)j * m], w.s.w[j], fit);
-            }
+            #pragma unroll 1
+            for (int j = 0; j < n; ++j) fit = fma(w.A[i + (long)j * m], w.s.w[j], fit);
             double bi = w.data[i] * mx;
             double ri = fit - bi;
             res[t] = ri;
@@ -1218,7 +1209,7 @@ static __device__ void process_voxel(Warp &w, long v) {
     for (int j = lane; j < n; j += 32) P.dist[v + P.V * j] = w.s.w[j];
     if (P.basis_out && P.angle_mode != 1)
         #pragma unroll 1
-        for (long q = lane; q < (long)m * n; q += 32) P.basis_out[v + P.V * q] = (use_mixed(w) && w.Af) ? widen(w.Af[q]) : w.A[q];
+        for (long q = lane; q < (long)m * n; q += 32) P.basis_out[v + P.V * q] = w.A[q];
     if (lane == 0) {
         P.gdn[v] = sd;
         P.ggm[v] = pm_exp(lggm);
