@@ -682,8 +682,15 @@ static __device__ void reg_lcurve(Warp &w, double &mu_out, double &chi2_out) {
 }
 
 // ---- GCV (src/lsqnonneg.jl:1136-1341) ----
-// Singular values of the m x n basis by one-sided Hestenes-Jacobi in shared
-// memory (stand-in for LAPACK dgesdd job 'N'), sorted descending into gam.
+// Singular values of the m x n basis (stand-in for LAPACK dgesdd job 'N',
+// src/utils.jl:67-134): Golub-Kahan Householder bidiagonalization of
+// B = A (m >= n) or A' (r x c, r >= c) in shared memory, then bisection on the
+// Golub-Kahan tridiagonal (zero diagonal, off-diagonals d0, e0, d1, e1, ...,
+// d_{c-1}), whose positive eigenvalues are the singular values, resolved to
+// 1e-15 of their Gershgorin bound; written descending to gam.  Every sum runs
+// sequentially in one lane (each lane its own columns or rows; the reflector
+// norms redundantly on every lane) and the bisection takes one singular value
+// per lane, so the oracle repeats it operation for operation.
 static __device__ void warp_svdvals(Warp &w, double *gam) {
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lane = w.lane;
@@ -695,59 +702,133 @@ static __device__ void warp_svdvals(Warp &w, double *gam) {
         #pragma unroll 1
         for (int i = lane; i < r; i += 32) U[i + (long)j * ld] = (m >= n) ? w.A[i + (long)j * m] : w.A[j + (long)i * m];
     __syncwarp();
-    const double EPS = 2.220446049250313e-16;
+    double *dv = w.s.zz, *ev = w.s.b;  // bidiagonal: c diagonal, c-1 superdiagonal entries
     #pragma unroll 1
-    for (int sweep = 0; sweep < 60; ++sweep) {
-        double off = 0;
+    for (int k = 0; k < c; ++k) {
+        const double *uk = U + (long)k * ld;
+        // left reflector H = I - tau v v', v = (x0 - alpha, x_{k+1..r-1}), on column k
+        double ss = 0.0;
         #pragma unroll 1
-        for (int p = 0; p < c - 1; ++p) {
+        for (int i = k + 1; i < r; ++i) ss = fma(uk[i], uk[i], ss);
+        const double x0 = uk[k];
+        double alpha = x0, v0 = 0.0, tau = 0.0;
+        if (ss != 0.0) {
+            const double nrm = sqrt(fma(x0, x0, ss));
+            alpha = x0 >= 0.0 ? -nrm : nrm;
+            v0 = x0 - alpha;
+            tau = 2.0 / fma(v0, v0, ss);
+        }
+        if (lane == 0) dv[k] = alpha;
+        if (tau != 0.0) {
             #pragma unroll 1
-            for (int q = p + 1; q < c; ++q) {
-                double *up = U + (long)p * ld, *uq = U + (long)q * ld;
-                double pa = 0, pb = 0, pg = 0;
+            for (int j = k + 1 + lane; j < c; j += 32) {
+                double *uj = U + (long)j * ld;
+                double sdot = v0 * uj[k];
                 #pragma unroll 1
-                for (int i = lane; i < r; i += 32) {
-                    double x = up[i], y = uq[i];
-                    pa = fma(x, x, pa); pb = fma(y, y, pb); pg = fma(x, y, pg);
-                }
-                double al = wsum(pa), be = wsum(pb), ga = wsum(pg);
-                if (ga == 0 || fabs(ga) <= EPS * sqrt(al * be)) continue;
-                double rel = fabs(ga) / sqrt(al * be);
-                off = rel > off ? rel : off;
-                double zeta = (be - al) / (2 * ga);
-                double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1 + zeta * zeta));
-                double cs = 1 / sqrt(1 + t * t), sn = cs * t;
+                for (int i = k + 1; i < r; ++i) sdot = fma(uk[i], uj[i], sdot);
+                const double f = tau * sdot;
+                uj[k] = fma(-f, v0, uj[k]);
                 #pragma unroll 1
-                for (int i = lane; i < r; i += 32) {
-                    double x = up[i], y = uq[i];
-                    up[i] = cs * x - sn * y;
-                    uq[i] = sn * x + cs * y;
-                }
-                __syncwarp();
+                for (int i = k + 1; i < r; ++i) uj[i] = fma(-f, uk[i], uj[i]);
             }
         }
-        if (off <= EPS) break;
+        __syncwarp();
+        if (k + 2 < c) {
+            // right reflector on row k, columns k+1..c-1
+            double sr = 0.0;
+            #pragma unroll 1
+            for (int j = k + 2; j < c; ++j) { const double y = U[k + (long)j * ld]; sr = fma(y, y, sr); }
+            const double y0 = U[k + (long)(k + 1) * ld];
+            double beta = y0, w0 = 0.0, tau2 = 0.0;
+            if (sr != 0.0) {
+                const double nrm = sqrt(fma(y0, y0, sr));
+                beta = y0 >= 0.0 ? -nrm : nrm;
+                w0 = y0 - beta;
+                tau2 = 2.0 / fma(w0, w0, sr);
+            }
+            if (lane == 0) ev[k] = beta;
+            if (tau2 != 0.0) {
+                #pragma unroll 1
+                for (int i = k + 1 + lane; i < r; i += 32) {
+                    double sdot = w0 * U[i + (long)(k + 1) * ld];
+                    #pragma unroll 1
+                    for (int j = k + 2; j < c; ++j) sdot = fma(U[k + (long)j * ld], U[i + (long)j * ld], sdot);
+                    const double f = tau2 * sdot;
+                    U[i + (long)(k + 1) * ld] = fma(-f, w0, U[i + (long)(k + 1) * ld]);
+                    #pragma unroll 1
+                    for (int j = k + 2; j < c; ++j) U[i + (long)j * ld] = fma(-f, U[k + (long)j * ld], U[i + (long)j * ld]);
+                }
+            }
+            __syncwarp();
+        } else if (k + 1 < c) {
+            if (lane == 0) ev[k] = U[k + (long)(k + 1) * ld];
+            __syncwarp();
+        }
     }
-    // column norms, then rank-sort descending
-    double *tmp = w.s.zz;
+    // Golub-Kahan tridiagonal: squared off-diagonals o2 (2c-1, in U's storage)
+    // and the Gershgorin bound
+    const int N = 2 * c;
+    double *o2 = U;
+    double bnd = 0.0;
     #pragma unroll 1
-    for (int j = 0; j < c; ++j) {
-        const double *u = U + (long)j * ld;
-        double part = 0;
-        #pragma unroll 1
-        for (int i = lane; i < r; i += 32) part = fma(u[i], u[i], part);
-        double sv = sqrt(wsum(part));
-        if (lane == 0) tmp[j] = sv;
+    for (int j = lane; j < N; j += 32) {
+        const double oa = j > 0 ? fabs((j - 1) % 2 == 0 ? dv[(j - 1) / 2] : ev[(j - 1) / 2]) : 0.0;
+        const double ob = j + 1 < N ? fabs(j % 2 == 0 ? dv[j / 2] : ev[j / 2]) : 0.0;
+        bnd = fmax(bnd, oa + ob);
     }
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) bnd = fmax(bnd, __shfl_xor_sync(FULL, bnd, o));
     __syncwarp();
     #pragma unroll 1
-    for (int j = lane; j < c; j += 32) {
-        double v = tmp[j];
-        int rank = 0;
-        #pragma unroll 1
-        for (int k = 0; k < c; ++k) rank += (tmp[k] > v) || (tmp[k] == v && k < j);
-        gam[rank] = v;
+    for (int j = lane; j + 1 < N; j += 32) {
+        const double o = j % 2 == 0 ? dv[j / 2] : ev[j / 2];
+        o2[j] = o * o;
     }
+    __syncwarp();
+    const double tau0 = 1e-14 * bnd, atol = 1e-15 * bnd;
+    // Sturm count: eigenvalues of the tridiagonal below x (zero diagonal)
+    auto count_below = [&](double x) {
+        double p2 = 1.0, p1 = 0.0 - x;
+        bool neg = p1 <= 0;  // a zero takes the sign opposite to its predecessor (p_0 = +1)
+        int cnt = neg;
+        #pragma unroll 1
+        for (int j = 1; j < N; ++j) {
+            double p = fma(0.0 - x, p1, -o2[j - 1] * p2);
+            bool pneg = p < 0 || (p == 0 && !neg);
+            cnt += (pneg != neg);
+            neg = pneg;
+            p2 = p1;
+            p1 = p;
+            const int ex = ((__double2hiint(p1) >> 20) & 0x7ff) - 1023;
+            if (p1 != 0 && (ex > 400 || ex < -400)) {
+                const double sc = __hiloint2double((1023 - ex) << 20, 0);
+                p1 *= sc;
+                p2 *= sc;
+            }
+        }
+        return cnt;
+    };
+    const int nres = N - count_below(tau0);  // singular values >= tau0 (the rest are left at zero)
+    #pragma unroll 1
+    for (int base = 0; base < nres; base += 32) {
+        const int t = base + lane;  // t-th largest singular value
+        const bool mine = t < nres;
+        const int idx = N - 1 - t;  // its index among the eigenvalues in ascending order
+        double a = tau0, b = bnd;
+        bool done = !mine;
+        #pragma unroll 1
+        for (int it = 0; it < 80 && __any_sync(FULL, !done); ++it) {
+            const double mid = 0.5 * (a + b);
+            const int cnt = count_below(mid);
+            if (!done) {
+                if (cnt > idx) b = mid; else a = mid;
+                done = (b - a) <= fmax(atol, 4.0 * 2.220446049250313e-16 * b);
+            }
+        }
+        if (mine && t < c) gam[t] = 0.5 * (a + b);
+    }
+    #pragma unroll 1
+    for (int t = nres + lane; t < c; t += 32) gam[t] = 0.0;
     __syncwarp();
 }
 struct GcvF {  // log𝒢(logμ), src/lsqnonneg.jl:1150-1154 and gcv!, 1213-1229

@@ -1215,57 +1215,127 @@ void orc_brent_minimize(orc_fn f, void *ctx, double a, double b, double xatol, d
 
 /* ------------------------------------------------------------------------- */
 /* Singular values (stand-in for LAPACK dgesdd job='N', src/utils.jl:67-134)  */
-/* One-sided Hestenes-Jacobi on the columns of A (or of A' when m < n).       */
+/* Householder bidiagonalization + bisection on the Golub-Kahan tridiagonal.  */
 /* ------------------------------------------------------------------------- */
-static int cmp_desc(const void *a, const void *b) {
-    double x = *(const double *)a, y = *(const double *)b;
-    return (x < y) - (x > y);
+/* Golub-Kahan Householder bidiagonalization of B = A (m >= n) or A' (r x c,
+ * r >= c), then bisection on the Golub-Kahan tridiagonal (zero diagonal,
+ * off-diagonals d0, e0, d1, e1, ..., d_{c-1}) whose positive eigenvalues are
+ * the singular values, resolved to 1e-15 of their Gershgorin bound; sorted
+ * descending.  The GPU path (warp_svdvals) performs the same operations in the
+ * same order: sequential sums, FMAs and IEEE square roots and divisions. */
+static int sturm_count_gk(const double *o2, int N, double x) {
+    double p2 = 1.0, p1 = 0.0 - x;
+    int neg = p1 <= 0;
+    int cnt = neg;
+    for (int j = 1; j < N; ++j) {
+        double p = fma(0.0 - x, p1, -o2[j - 1] * p2);
+        int pneg = p < 0 || (p == 0 && !neg);
+        cnt += (pneg != neg);
+        neg = pneg;
+        p2 = p1;
+        p1 = p;
+        uint64_t u;
+        memcpy(&u, &p1, 8);
+        const int ex = (int)((u >> 52) & 0x7ff) - 1023;
+        if (p1 != 0 && (ex > 400 || ex < -400)) {
+            const uint64_t su = (uint64_t)(uint32_t)((1023 - ex) << 20) << 32;
+            double sc;
+            memcpy(&sc, &su, 8);
+            p1 *= sc;
+            p2 *= sc;
+        }
+    }
+    return cnt;
 }
-static void jacobi_svdvals(const double *A, int m, int n, double *s, double *U) {
-    int r = m >= n ? m : n, c = m >= n ? n : m; /* U is r x c with c <= r */
+static void bidiag_svdvals(const double *A, int m, int n, double *s, double *U) {
+    const int r = m >= n ? m : n, c = m >= n ? n : m; /* U is r x c with c <= r */
     for (int j = 0; j < c; ++j)
         for (int i = 0; i < r; ++i) U[i + (size_t)j * r] = (m >= n) ? A[i + (size_t)j * m] : A[j + (size_t)i * m];
-    for (int sweep = 0; sweep < 60; ++sweep) {
-        double off = 0;
-        for (int p = 0; p < c - 1; ++p) {
-            for (int q = p + 1; q < c; ++q) {
-                double *up = U + (size_t)p * r, *uq = U + (size_t)q * r;
-                lacc La = {{0}}, Lb = {{0}}, Lc = {{0}};
-                for (int i = 0; i < r; ++i) {
-                    La.p[i & 31] = fma(up[i], up[i], La.p[i & 31]);
-                    Lb.p[i & 31] = fma(uq[i], uq[i], Lb.p[i & 31]);
-                    Lc.p[i & 31] = fma(up[i], uq[i], Lc.p[i & 31]);
-                }
-                double al = lacc_tree(&La), be = lacc_tree(&Lb), ga = lacc_tree(&Lc);
-                FL(6.0 * r);
-                if (ga == 0 || fabs(ga) <= EPS64 * sqrt(al * be)) continue;
-                double rel = fabs(ga) / sqrt(al * be);
-                if (rel > off) off = rel;
-                double zeta = (be - al) / (2 * ga);
-                double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1 + zeta * zeta));
-                double cs = 1 / sqrt(1 + t * t), sn = cs * t;
-                for (int i = 0; i < r; ++i) {
-                    double a = up[i], b = uq[i];
-                    up[i] = cs * a - sn * b;
-                    uq[i] = sn * a + cs * b;
-                }
-                FL(6.0 * r + 12);
-            }
+    double *dv = (double *)malloc(sizeof(double) * (2 * (size_t)c + 1)), *ev = dv + c;
+    for (int k = 0; k < c; ++k) {
+        const double *uk = U + (size_t)k * r;
+        double ss = 0.0;
+        for (int i = k + 1; i < r; ++i) ss = fma(uk[i], uk[i], ss);
+        const double x0 = uk[k];
+        double alpha = x0, v0 = 0.0, tau = 0.0;
+        if (ss != 0.0) {
+            const double nrm = sqrt(fma(x0, x0, ss));
+            alpha = x0 >= 0.0 ? -nrm : nrm;
+            v0 = x0 - alpha;
+            tau = 2.0 / fma(v0, v0, ss);
         }
-        if (off <= EPS64) break;
+        dv[k] = alpha;
+        if (tau != 0.0) {
+            for (int j = k + 1; j < c; ++j) {
+                double *uj = U + (size_t)j * r;
+                double sdot = v0 * uj[k];
+                for (int i = k + 1; i < r; ++i) sdot = fma(uk[i], uj[i], sdot);
+                const double f = tau * sdot;
+                uj[k] = fma(-f, v0, uj[k]);
+                for (int i = k + 1; i < r; ++i) uj[i] = fma(-f, uk[i], uj[i]);
+            }
+            FL(4.0 * (r - k) * (c - k - 1));
+        }
+        if (k + 2 < c) {
+            double sr = 0.0;
+            for (int j = k + 2; j < c; ++j) { const double y = U[k + (size_t)j * r]; sr = fma(y, y, sr); }
+            const double y0 = U[k + (size_t)(k + 1) * r];
+            double beta = y0, w0 = 0.0, tau2 = 0.0;
+            if (sr != 0.0) {
+                const double nrm = sqrt(fma(y0, y0, sr));
+                beta = y0 >= 0.0 ? -nrm : nrm;
+                w0 = y0 - beta;
+                tau2 = 2.0 / fma(w0, w0, sr);
+            }
+            ev[k] = beta;
+            if (tau2 != 0.0) {
+                for (int i = k + 1; i < r; ++i) {
+                    double sdot = w0 * U[i + (size_t)(k + 1) * r];
+                    for (int j = k + 2; j < c; ++j) sdot = fma(U[k + (size_t)j * r], U[i + (size_t)j * r], sdot);
+                    const double f = tau2 * sdot;
+                    U[i + (size_t)(k + 1) * r] = fma(-f, w0, U[i + (size_t)(k + 1) * r]);
+                    for (int j = k + 2; j < c; ++j) U[i + (size_t)j * r] = fma(-f, U[k + (size_t)j * r], U[i + (size_t)j * r]);
+                }
+                FL(4.0 * (r - k - 1) * (c - k - 1));
+            }
+        } else if (k + 1 < c) {
+            ev[k] = U[k + (size_t)(k + 1) * r];
+        }
     }
-    for (int j = 0; j < c; ++j) {
-        lacc Ls = {{0}};
-        const double *u = U + (size_t)j * r;
-        for (int i = 0; i < r; ++i) Ls.p[i & 31] = fma(u[i], u[i], Ls.p[i & 31]);
-        s[j] = sqrt(lacc_tree(&Ls));
+    const int N = 2 * c;
+    double bnd = 0.0;
+    for (int j = 0; j < N; ++j) {
+        const double oa = j > 0 ? fabs((j - 1) % 2 == 0 ? dv[(j - 1) / 2] : ev[(j - 1) / 2]) : 0.0;
+        const double ob = j + 1 < N ? fabs(j % 2 == 0 ? dv[j / 2] : ev[j / 2]) : 0.0;
+        bnd = fmax(bnd, oa + ob);
     }
-    qsort(s, c, sizeof(double), cmp_desc);
+    double *o2 = U;
+    for (int j = 0; j + 1 < N; ++j) {
+        const double o = j % 2 == 0 ? dv[j / 2] : ev[j / 2];
+        o2[j] = o * o;
+    }
+    const double tau0 = 1e-14 * bnd, atol = 1e-15 * bnd;
+    const int nres = N - sturm_count_gk(o2, N, tau0);
+    for (int t = 0; t < c; ++t) {
+        if (t >= nres) { s[t] = 0.0; continue; }
+        const int idx = N - 1 - t;
+        double a = tau0, b = bnd;
+        int done = 0;
+        for (int it = 0; it < 80 && !done; ++it) {
+            const double mid = 0.5 * (a + b);
+            const int cnt = sturm_count_gk(o2, N, mid);
+            if (cnt > idx) b = mid; else a = mid;
+            done = (b - a) <= fmax(atol, 4.0 * 2.220446049250313e-16 * b);
+            FL(3.0 * N);
+        }
+        s[t] = 0.5 * (a + b);
+    }
+    free(dv);
 }
 int orc_svdvals(const double *A, int m, int n, double *s) {
     int r = m >= n ? m : n, c = m >= n ? n : m;
     double *U = (double *)malloc(sizeof(double) * (size_t)r * c);
-    jacobi_svdvals(A, m, n, s, U);
+    bidiag_svdvals(A, m, n, s, U);
     free(U);
     return 0;
 }
@@ -1655,7 +1725,7 @@ static double gcv_logf(double logmu, void *ctx) {
 }
 static const double *reg_gcv(reg_ws *r, double *mu_out, double *chi2_out, int need_chi2) {
     g_st = ORC_ST_SVD;
-    jacobi_svdvals(r->A, r->m, r->n, r->gamma, r->svdU);
+    bidiag_svdvals(r->A, r->m, r->n, r->gamma, r->svdU);
     g_st = ORC_ST_REG_OTHER;
     double logmu, logG;
     brent_minimize(gcv_logf, r, -8.0, 2.0, 0.0, 1e-4, 20, &logmu, &logG);
