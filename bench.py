@@ -376,6 +376,7 @@ def run_serve_workload(args):
         # warm the bases and the kernels
         for name in pool:
             srv.result(srv.submit(*pool[name][0]))
+        srv.reset_stats()  # latency percentiles over the timed requests only
         st0 = srv.stats()
         ids, t_sub = [], []
         picks = rng.choice(len(kinds), size=args.requests, p=[k[3] for k in kinds])

@@ -1796,6 +1796,16 @@ extern "C" int decaes_server_get_stats(decaes_server *S, decaes_server_stats *ou
     return DECAES_OK;
 }
 
+extern "C" int decaes_server_reset_stats(decaes_server *S) {
+    if (!S) return DECAES_EINVAL;
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->lat_ms.clear();
+    S->submitted = S->completed = S->failed = S->voxels = S->ticks = 0;
+    S->busy_ms = 0;
+    S->t0 = Clock::now();
+    return DECAES_OK;
+}
+
 extern "C" void decaes_server_destroy(decaes_server *S) {
     if (!S) return;
     {

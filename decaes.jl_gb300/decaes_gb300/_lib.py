@@ -82,7 +82,7 @@ EXPORTS = ["decaes_create", "decaes_destroy", "decaes_last_error", "decaes_get_s
            "decaes_t2map_t2part_device", "decaes_sync_stats", "decaes_mock_image", "decaes_t2map_t2part_noalloc",
            "decaes_t2map_t2part_batch", "decaes_batch_create", "decaes_batch_run", "decaes_batch_destroy",
            "decaes_autotune", "decaes_server_create", "decaes_server_submit", "decaes_server_poll",
-           "decaes_server_wait", "decaes_server_get_stats", "decaes_server_destroy"]
+           "decaes_server_wait", "decaes_server_get_stats", "decaes_server_reset_stats", "decaes_server_destroy"]
 
 _lib = None
 
@@ -134,6 +134,7 @@ def load(build_if_needed: bool = True):
     L.decaes_server_poll.argtypes = [_vp, C.c_int64]
     L.decaes_server_wait.argtypes = [_vp, C.c_int64]
     L.decaes_server_get_stats.argtypes = [_vp, C.POINTER(ServerStatsC)]
+    L.decaes_server_reset_stats.argtypes = [_vp]
     L.decaes_server_destroy.argtypes = [_vp]
     _lib = L
     return L

@@ -72,6 +72,10 @@ class Server:
         self.L.decaes_server_get_stats(self.h, C.byref(st))
         return {k: getattr(st, k) for k, _ in _lib.ServerStatsC._fields_}
 
+    def reset_stats(self):
+        """Clears the counters and latency samples (after warm-up requests)."""
+        self.L.decaes_server_reset_stats(self.h)
+
     def close(self):
         if getattr(self, "h", None):
             self.L.decaes_server_destroy(self.h)

@@ -248,6 +248,9 @@ int decaes_server_poll(decaes_server *srv, int64_t id);
 /* Blocks until the request is done; returns DECAES_OK or its error code. */
 int decaes_server_wait(decaes_server *srv, int64_t id);
 int decaes_server_get_stats(decaes_server *srv, decaes_server_stats *out);
+/* Clears the counters and latency samples (e.g. after warm-up requests); the
+ * requests in flight are counted when they finish. */
+int decaes_server_reset_stats(decaes_server *srv);
 /* Finishes every queued request, then stops the scheduler and frees the server. */
 void decaes_server_destroy(decaes_server *srv);
 

@@ -79,3 +79,21 @@ def test_admission_by_footprint(D, ctx):
         srv.close()
     for a, b in zip(got, alone):
         _same(a, b)
+
+
+def test_reset_stats(D, ctx):
+    """Counters and latency samples restart after reset_stats (warm-up excluded from percentiles)."""
+    from decaes_gb300.server import Server
+    img, mo, po = _req(D, REQS[3])
+    srv = Server(ctx)
+    try:
+        srv.result(srv.submit(img, mo, po))
+        assert srv.stats()["completed"] == 1
+        srv.reset_stats()
+        st = srv.stats()
+        assert st["completed"] == 0 and st["p50_ms"] == 0 and st["voxels"] == 0
+        srv.result(srv.submit(img, mo, po))
+        st = srv.stats()
+        assert st["completed"] == 1 and st["p50_ms"] > 0 and st["voxels"] == int(np.prod(REQS[3]["X"]))
+    finally:
+        srv.close()
