@@ -428,7 +428,7 @@ int make_params(decaes_ctx *ctx, const decaes_t2map_opts &o, const dh::T2partPla
         const long rr = dk::mixed_r1_doubles(m, n) + dk::mixed_r2_doubles(m, n, o.Reg == DECAES_REG_GCV);
         P.epg_lanes_f32 = (int)std::max<long>(1, std::min<long>(32, 2 * rr / (3L * m)));
     }
-    P.epg_lanes = (int)std::min<long>(32, ((long)P.lda * n) / (3L * m));
+    P.epg_lanes = dk::fp64_epg_lanes(m, n, P.lda);
     P.scr_stride = dk::warp_scratch_doubles(m, n, P.K);
     *wsm = mixed ? dk::warp_smem_doubles_mixed(m, n, o.Reg == DECAES_REG_GCV) : dk::warp_smem_doubles(m, n, P.lda);
     *wsm = (*wsm + 1) & ~1L;  // 16-byte aligned warp workspaces

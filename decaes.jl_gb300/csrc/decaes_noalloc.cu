@@ -267,7 +267,7 @@ extern "C" int decaes_t2map_t2part_noalloc(const decaes_t2map_opts *mopts, const
         P.weights = pp.weights.empty() ? nullptr : dptr(o_w);
         P.sfr = (double *)d_pout->sfr; P.sgm = (double *)d_pout->sgm; P.mfr = (double *)d_pout->mfr; P.mgm = (double *)d_pout->mgm;
     }
-    P.epg_lanes = (int)std::min<long>(32, ((long)P.lda * n) / (3L * m));
+    P.epg_lanes = dk::fp64_epg_lanes(m, n, P.lda);
     P.scratch = dptr(o_scr);
     kern<<<grid, 32, smem, st>>>(P);
     NA_CK(cudaGetLastError());

@@ -1106,7 +1106,7 @@ static __device__ double flip_angle_search(Warp &w) {
 static __device__ void warp_basis(Warp &w, double alpha, double *out /* m x n, global */) {
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lanes = P.epg_lanes, lane = w.lane;
-    double *S = w.s.C;  // 3*m*lanes doubles, lane-contiguous
+    double *S = w.s.C;  // 3*m*lanes doubles, lane-contiguous, over the C, b and zz regions
     #pragma unroll 1
     for (int j0 = 0; j0 < n; j0 += lanes) {
         int j = j0 + lane;

@@ -83,6 +83,14 @@ __host__ __device__ inline long warp_smem_doubles_mixed(int m, int n, bool gcv) 
     long ints = 4L * n;  // idx, P, pos, lastP
     return d + (ints * 4 + 7) / 8;
 }
+// Lanes of the FP64 method's EPG basis (one T2 column per lane, 3m states
+// each).  The states use the contiguous C, b and zz regions of the workspace
+// (lda * (n + 2) doubles, free while the voxel's basis is built), which hold
+// at least one lane's states for every n >= 1 because lda >= m + n.
+__host__ __device__ inline int fp64_epg_lanes(int m, int n, int lda) {
+    long l = ((long)lda * (n + 2)) / (3L * m);
+    return (int)(l < 1 ? 1 : (l > 32 ? 32 : l));
+}
 // Global scratch of one warp worker (doubles).
 // Offset of the mixed method's FP32 basis (m x n floats) in it, after the
 // per-voxel basis, surrogate samples, L-curve caches, singular values and the
