@@ -11,7 +11,8 @@ test/cli.jl:318-328) and a T2part-only run on the saved distribution
 (test/cli.jl:339-348).  Here the oracle's outputs are checked for the
 invariants of the path on the CPU, and on the GPU the FP64 method is held to
 the oracle on every case, the B1 rerun and the standalone T2part to the fused
-run, and the saved per-voxel basis to the EPG curves at the fitted angle.
+run, and the saved per-voxel basis to the EPG curves at the fitted angle;
+the mixed method is held to its MWF gate on every case.
 (`Silent` and `Threaded` change no result and are left out.)"""
 import numpy as np
 import pytest
@@ -198,3 +199,28 @@ def test_gpu_sweep_matches_oracle(D, orc, ctx, name):
         assert e[okb].max() <= DIST_RTOL
         np.testing.assert_array_equal(maps_b1["alpha"], maps["alpha"])
         np.testing.assert_allclose(parts_b1["sfr"], parts["sfr"], rtol=0, atol=MWF_ATOL, equal_nan=True)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", NAMES)
+def test_gpu_sweep_mixed(D, orc, ctx, name):
+    """The mixed method on every case: the same voxels processed as the FP64
+    oracle, non-negative distributions, MWF within the method's gate (1e-3;
+    measured on a GB300: at most 6.3e-5 over the sweep) and flip angles
+    within 1e-2 degrees (measured: 1.3e-9)."""
+    s = settings(name)
+    img = image(D, s, seed=NAMES.index(name))
+    mo, po = options(D, s, precision="mixed")
+    maps, dist, parts = D.T2mapSEcorr_T2partSEcorr(img, mo, po, ctx=ctx)
+    om, od, op = oracle_run(orc, img, mo, po)
+    np.testing.assert_array_equal(np.isnan(dist), np.isnan(od))
+    np.testing.assert_array_equal(np.isnan(maps["alpha"]), np.isnan(om["alpha"]))
+    done = ~np.isnan(od).any(axis=-1)
+    assert (dist[done] >= 0).all()
+    if done.any():
+        d_mwf = np.abs(parts["sfr"] - op["sfr"])[~np.isnan(op["sfr"])]
+        d_alpha = np.abs(maps["alpha"] - om["alpha"])[done]
+        print(f"SWEEP_MIXED {name} voxels={int(done.sum())} mwf_max={d_mwf.max():.3e} "
+              f"mwf_median={np.median(d_mwf):.3e} alpha_max={d_alpha.max():.3e}")
+        assert d_mwf.max() <= 1e-3
+        assert d_alpha.max() <= 1e-2
