@@ -224,3 +224,54 @@ def test_gpu_sweep_mixed(D, orc, ctx, name):
               f"mwf_median={np.median(d_mwf):.3e} alpha_max={d_alpha.max():.3e}")
         assert d_mwf.max() <= 1e-3
         assert d_alpha.max() <= 1e-2
+
+
+# Corners of the supported shapes: the fewest echoes, T2 bins and angles the
+# options allow, and the most this library supports (nTE <= 128, nT2 <= 64
+# for the mixed method, nRefAngles <= 256).
+EXTREMES = {
+    "min": dict(nTE=4, nT2=2, nRefAngles=2, nRefAnglesMin=2),
+    "min_m_max_n": dict(nTE=4, nT2=64, nRefAngles=8),
+    "max_m_min_n": dict(nTE=128, nT2=2, nRefAngles=8),
+    "max": dict(nTE=128, nT2=64, nRefAngles=256),
+    "max_legacy": dict(nTE=128, nT2=64, nRefAngles=256, legacy=True, Reg="chi2", RegParams=1.02, Threshold=0.0),
+}
+
+
+def extreme_settings(name):
+    s = dict(DEFAULTS)
+    if EXTREMES[name].get("legacy"):
+        s.update(LEGACY_DEFAULTS)
+    s.update(EXTREMES[name])
+    return s
+
+
+@pytest.mark.parametrize("name", list(EXTREMES))
+def test_oracle_extreme_shapes(D, orc, name):
+    s = extreme_settings(name)
+    img = image(D, s, seed=7)
+    mo, po = options(D, s)
+    om, od, op = oracle_run(orc, img, mo, po)
+    assert not np.isnan(od).any() and (od >= 0).all()
+    assert ((om["alpha"] >= mo.MinRefAngle) & (om["alpha"] <= 180.0)).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(EXTREMES))
+def test_gpu_extreme_shapes(D, orc, ctx, name):
+    """Both methods at the corners: FP64 within the stated tolerances of the
+    oracle, the mixed method within its MWF gate."""
+    s = extreme_settings(name)
+    img = image(D, s, seed=7)
+    mo, po = options(D, s)
+    om, od, op = oracle_run(orc, img, mo, po)
+    maps, dist, parts = D.T2mapSEcorr_T2partSEcorr(img, mo, po, ctx=ctx)
+    err, ok = dist_rel_err(dist, od)
+    assert ok.all() and err.max() <= DIST_RTOL
+    assert np.abs(parts["sfr"] - op["sfr"]).max() <= MWF_ATOL
+    mo_x, po_x = options(D, s, precision="mixed")
+    maps_x, dist_x, parts_x = D.T2mapSEcorr_T2partSEcorr(img, mo_x, po_x, ctx=ctx)
+    assert not np.isnan(dist_x).any() and (dist_x >= 0).all()
+    d_mwf = np.abs(parts_x["sfr"] - op["sfr"])
+    print(f"EXTREME {name} mwf_max_mixed={d_mwf.max():.3e}")
+    assert d_mwf.max() <= 1e-3
