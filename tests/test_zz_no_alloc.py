@@ -144,3 +144,20 @@ def test_noalloc_argument_errors(D):
     assert L.decaes_t2map_t2part_noalloc(C.byref(bad), None, C.c_void_p(8), D_lib().F64, None, C.byref(mc),
                                          None, None, err, len(err)) == 1
     assert err.value.decode() == "At least four echoes are required for T2 mapping, but nTE = 3."
+
+
+@pytest.mark.parametrize("field,value,msg", [
+    ("nTE", 129, "nTE > 128 is not supported by libdecaes_gpu"),
+    ("nRefAngles", 257, "nRefAngles > 256 is not supported by libdecaes_gpu"),
+])
+def test_noalloc_shape_limits(D, field, value, msg):
+    """Shapes beyond the library's limits are rejected on the host, before any
+    CUDA call (no GPU needed)."""
+    L = D.load()
+    err = C.create_string_buffer(256)
+    o = D.T2mapOptions(MatrixSize=(2, 2, 1), nTE=32, TE=10e-3, nT2=40, T2Range=(10e-3, 2.0), Reg="lcurve").to_c()
+    setattr(o, field, value)
+    mc = D_lib().T2mapOutC(dist=8, gdn=8, ggm=8, gva=8, fnr=8, snr=8, alpha=8)
+    assert L.decaes_t2map_t2part_noalloc(C.byref(o), None, C.c_void_p(8), D_lib().F64, None, C.byref(mc),
+                                         None, None, err, len(err)) == 1
+    assert err.value.decode() == msg
