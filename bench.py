@@ -48,6 +48,9 @@ THRESHOLD = 200.0
 WORKLOADS = {
     "lcurve48": dict(matrix=(240, 240, 48), nTE=48, TE=10e-3, nT2=40, T2Range=(10e-3, 2.0), Reg="lcurve", K=32),
     "gcv56": dict(matrix=(240, 240, 113), nTE=56, TE=7e-3, nT2=60, T2Range=(8e-3, 2.0), Reg="gcv", K=64),
+    # the 48-echo volume with the MATLAB toolbox's regularization (chi2 1.02) and angle count (8)
+    "chi2k8_48": dict(matrix=(240, 240, 48), nTE=48, TE=10e-3, nT2=40, T2Range=(10e-3, 2.0), Reg="chi2",
+                      Chi2Factor=1.02, K=8),
 }
 
 
@@ -55,7 +58,8 @@ def workload(matrix, precision, name="lcurve48"):
     import decaes_gb300 as D
     w = WORKLOADS[name]
     mo = D.T2mapOptions(MatrixSize=matrix, nTE=w["nTE"], TE=w["TE"], nT2=w["nT2"], T2Range=w["T2Range"], Reg=w["Reg"],
-                        nRefAngles=w["K"], MinRefAngle=50.0, Threshold=THRESHOLD, precision=precision)
+                        nRefAngles=w["K"], MinRefAngle=50.0, Threshold=THRESHOLD, Chi2Factor=w.get("Chi2Factor"),
+                        precision=precision)
     po = D.T2partOptions.from_t2map(mo, SPWin=SPWIN, MPWin=MPWIN)
     mock = D.MockImageOptions(MatrixSize=matrix, nTE=w["nTE"], TE=w["TE"], BackgroundFraction=0.35)
     return mo, po, mock
@@ -67,7 +71,7 @@ def config_dict(matrix, precision, V, Vp, name="lcurve48"):
     return {
         "workload": f"{matrix[0]}x{matrix[1]}x{matrix[2]} voxels x {w['nTE']} echoes, TE={w['TE'] * 1e3:g}ms, "
                     f"nT2={w['nT2']} ({w['T2Range'][0] * 1e3:g}ms-{w['T2Range'][1]:g}s), nRefAngles={w['K']} "
-                    f"(spline flip-angle search), Reg={w['Reg']}, Float32 input, T2part SPWin 10-25ms MPWin 25-200ms",
+                    f"(spline flip-angle search), Reg={w['Reg']}{' ' + str(w['Chi2Factor']) if 'Chi2Factor' in w else ''}, Float32 input, T2part SPWin 10-25ms MPWin 25-200ms",
         "precision": precision,
         "voxels": V,
         "voxels_above_threshold": Vp,
