@@ -226,3 +226,36 @@ def test_oracle_pipeline_small(orc):
     parts = orc.t2part(dist, orc.T2partOptions(MatrixSize=X, nT2=40, T2Range=(10e-3, 2.0), SPWin=(10e-3, 25e-3),
                                                MPWin=(25e-3, 200e-3)))
     assert np.all((parts["sfr"] > 0.05) & (parts["sfr"] < 0.3))
+
+
+# ---- non-finite echoes (bad per-voxel inputs) --------------------------------
+@pytest.mark.parametrize("reg,kw", [("none", {}), ("chi2", dict(Chi2Factor=1.02)), ("lcurve", {}), ("gcv", {}),
+                                    ("mdp", dict(NoiseLevel=1.0))])
+def test_nonfinite_echoes(orc, reg, kw):
+    """NaN and Inf echoes end in bounded time and stay within their voxel,
+    following src/T2mapSEcorr.jl:201-218: the threshold test `image[I, 1] >
+    Threshold` skips a NaN first echo; the running maximum
+    `b > max ? b : max` passes over a NaN later echo (the voxel is processed
+    with a finite, non-negative distribution); an Inf echo makes the maximum
+    Inf and the rescaled distribution NaN (0 * Inf)."""
+    rng = np.random.default_rng(1)
+    m, X = 32, (4, 1, 1)
+    img = np.empty(X + (m,))
+    for v in np.ndindex(X):
+        img[v] = 1000 * orc.epg_decay_curve(m, 160.0, 10e-3, 60e-3, 1.0) + rng.normal(0, 2.0, m)
+    clean = img[3:4].copy()
+    img[0, 0, 0, 5] = np.nan
+    img[1, 0, 0, 3] = np.inf
+    img[2, 0, 0, 0] = np.nan
+    o = orc.T2mapOptions(MatrixSize=X, nTE=m, TE=10e-3, nT2=40, T2Range=(10e-3, 2.0), Reg=reg, nRefAngles=8,
+                         SaveRegParam=True, **kw)
+    maps, dist = orc.t2map(img, o)
+    assert np.isfinite(dist[0, 0, 0]).all() and (dist[0, 0, 0] >= 0).all()
+    assert np.isnan(dist[1, 0, 0]).all()
+    assert np.isnan(dist[2, 0, 0]).all() and np.isnan(maps["alpha"][2, 0, 0])
+    o1 = orc.T2mapOptions(MatrixSize=(1, 1, 1), nTE=m, TE=10e-3, nT2=40, T2Range=(10e-3, 2.0), Reg=reg, nRefAngles=8,
+                          SaveRegParam=True, **kw)
+    maps1, dist1 = orc.t2map(clean, o1)
+    np.testing.assert_array_equal(dist[3:4], dist1)
+    for k in maps1:
+        np.testing.assert_array_equal(maps[k][3:4], maps1[k], err_msg=k)
