@@ -548,6 +548,8 @@ def main():
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    # above-threshold voxels per second (rank 0's count times the ranks)
+    line["config"]["voxels_above_threshold_per_s"] = world * Vp / (ms_per_step * 1e-3)
     if compare is not None:
         line["mixed_vs_fp64"] = compare
     # ---- roofline of the voxel-solve kernel and the CPU baseline ----
