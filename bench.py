@@ -13,11 +13,16 @@ threshold.  A step is one pass of T2map+T2part over the whole volume.
   e2e    the same metric through the host-buffer C ABI call from pinned
          memory (H2D of the image and D2H of all outputs inside the timing)
   mixed_vs_fp64  the FP64 (plain) method on the same volume: its voxels/s,
-         the speed-up, and |MWF_mixed - MWF_FP64| over every processed voxel
-         (the method's accuracy gate: p99 <= 1e-3)
+         the speed-up, and the mixed method's per-output error against it
+         over every processed voxel (MWF, distribution L1, flip angle; the
+         method's accuracy gate: MWF p99 <= 1e-3)
+  parity  the oracle (FP64 CPU restatement of the reference path) on a
+         sample of the volume's voxels against the FP64 GPU method (bitwise /
+         1e-8 per bin / 1e-10 MWF) and the mixed method (its gate)
   --precision fp64  makes the FP64 method the headline
   --impl reference  times the CPU restatement of the reference path (the
-         oracle, all host threads) on a bounded sample of the same workload.
+         oracle, all host threads) on a leading z-slab of the same volume,
+         generated without loading the GPU library.
 """
 from __future__ import annotations
 
@@ -54,6 +59,20 @@ WORKLOADS = {
 }
 
 
+# z-slices of one --impl reference step (about 5 s of oracle work on 16 cores)
+REF_SLICES = {"lcurve48": 2, "gcv56": 1, "chi2k8_48": 4}
+# The reference's published whole-dataset figures for these echo counts and
+# matrix sizes (README.md:72-73, DECAES on a 32-core AMD Threadripper 3970X;
+# real MSE data, settings and mask not stated): voxels / time.
+_PUB48 = {"value": 240 * 240 * 48 / 4.3, "unit": "voxels/s", "cores": 32,
+          "source": "README.md:73: 48-echo 240x240x48 dataset in 4.3 s on an AMD Threadripper 3970X (32 cores); "
+                    "settings and mask not stated"}
+PUBLISHED = {"lcurve48": _PUB48, "chi2k8_48": _PUB48,
+             "gcv56": {"value": 240 * 240 * 113 / 7.7, "unit": "voxels/s", "cores": 32,
+                       "source": "README.md:72: 56-echo 240x240x113 dataset in 7.7 s on an AMD Threadripper 3970X "
+                                 "(32 cores); settings and mask not stated"}}
+
+
 def workload(matrix, precision, name="lcurve48"):
     import decaes_gb300 as D
     w = WORKLOADS[name]
@@ -65,19 +84,238 @@ def workload(matrix, precision, name="lcurve48"):
     return mo, po, mock
 
 
-def config_dict(matrix, precision, V, Vp, name="lcurve48"):
+def config_dict(matrix, V, name="lcurve48"):
+    """The workload, identical in both arms' lines (nothing measured in it)."""
     w = WORKLOADS[name]
     img_mb = V * w["nTE"] * 4 / 1e6
     return {
         "workload": f"{matrix[0]}x{matrix[1]}x{matrix[2]} voxels x {w['nTE']} echoes, TE={w['TE'] * 1e3:g}ms, "
                     f"nT2={w['nT2']} ({w['T2Range'][0] * 1e3:g}ms-{w['T2Range'][1]:g}s), nRefAngles={w['K']} "
                     f"(spline flip-angle search), Reg={w['Reg']}{' ' + str(w['Chi2Factor']) if 'Chi2Factor' in w else ''}, Float32 input, T2part SPWin 10-25ms MPWin 25-200ms",
-        "precision": precision,
         "voxels": V,
-        "voxels_above_threshold": Vp,
         "l2": f"inputs larger than L2 ({img_mb:.0f} MB image vs 129 MB L2); no flush needed",
         "parallelism": "replicas (independent volume per GPU)",
     }
+
+
+def _oracle():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    return O
+
+
+def oracle_opts(O, name, V):
+    w = WORKLOADS[name]
+    return O.T2mapOptions(MatrixSize=(V, 1, 1), nTE=w["nTE"], TE=w["TE"], nT2=w["nT2"], T2Range=w["T2Range"],
+                          Reg=w["Reg"], nRefAngles=w["K"], MinRefAngle=50.0, Threshold=THRESHOLD,
+                          Chi2Factor=w.get("Chi2Factor"))
+
+
+def oracle_run(O, name, flat, threads):
+    """The oracle on voxel rows flat (V x nTE): T2map + T2part; returns
+    (maps, dist V x nT2, parts, FP64 FLOPs per processed voxel, seconds)."""
+    w = WORKLOADS[name]
+    V = flat.shape[0]
+    sub = np.asfortranarray(flat.astype(np.float64)).reshape((V, 1, 1, w["nTE"]), order="F")
+    t0 = time.perf_counter()
+    maps, dist, fl = O.t2map(sub, oracle_opts(O, name, V), nthreads=threads, return_flops=True)
+    parts = O.t2part(dist, O.T2partOptions(MatrixSize=(V, 1, 1), nT2=w["nT2"], T2Range=w["T2Range"], SPWin=SPWIN,
+                                           MPWin=MPWIN))
+    dt = time.perf_counter() - t0
+    nproc = max(1, int((~np.isnan(maps["alpha"].reshape(-1))).sum()))
+    flat_maps = {k: v.reshape(V, -1, order="F").squeeze(-1) if v.ndim == 3 else v for k, v in maps.items()}
+    return flat_maps, dist.reshape(V, w["nT2"], order="F"), {k: v.reshape(-1, order="F") for k, v in parts.items()}, \
+        sum(fl.values()) / nproc, dt
+
+
+def cpu_baseline(name, flat, Vp, sample, threads):
+    """The oracle on a bounded sample of above-threshold voxels (rows of flat,
+    V x nTE, evenly spread over the processed voxels); returns the voxel
+    indices, the oracle's outputs on them, voxels/s scaled to the whole image
+    (its time per processed voxel times the image's processed-voxel count) and
+    the FP64 FLOPs per processed voxel."""
+    O = _oracle()
+    fg = np.flatnonzero(flat[:, 0] > THRESHOLD)
+    pick = fg[np.linspace(0, len(fg) - 1, min(sample, len(fg))).astype(np.int64)]
+    maps, dist, parts, flv, dt = oracle_run(O, name, flat[pick], threads)
+    whole = dt / len(pick) * Vp
+    return dict(pick=pick, maps=maps, dist=dist, parts=parts, value=flat.shape[0] / whole, seconds=dt,
+                flops_per_voxel=flv)
+
+
+def run_reference(args):
+    """Times the oracle (CPU restatement of the reference path) on the host
+    cores.  Each step runs T2map + T2part on a leading z-slab of the
+    workload's volume (the first --ref-slices slices: the same voxels the
+    whole-volume run sees there), generated by the oracle's copy of the
+    synthetic generator, so nothing of the GPU library is loaded."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    O = _oracle()
+    w = WORKLOADS[args.workload]
+    matrix = tuple(args.matrix) if args.matrix else w["matrix"]
+    nz = max(1, min(args.ref_slices or REF_SLICES[args.workload], matrix[2]))
+    slab = (matrix[0], matrix[1], nz)
+    Vs = int(np.prod(slab))
+    threads = os.cpu_count() or 1
+    img = O.mock_image(slab, w["nTE"], seed=args.seed, dtype=np.float32, TE=w["TE"], BackgroundFraction=0.35,
+                       nthreads=threads)
+    flat = img.reshape((Vs, w["nTE"]), order="F")
+    nfg = int((flat[:, 0] > THRESHOLD).sum())
+    for _ in range(args.warmup):
+        oracle_run(O, args.workload, flat, threads)
+    secs = []
+    for _ in range(args.steps):
+        secs.append(oracle_run(O, args.workload, flat, threads)[4])
+    ms_per_step = 1e3 * sum(secs) / len(secs)
+    value = Vs / (ms_per_step * 1e-3)
+    V = int(np.prod(matrix))
+    sample = (f"each step: the first {nz} of {matrix[2]} z-slices of the volume ({slab[0]}x{slab[1]}x{nz} = {Vs} "
+              f"voxels, {nfg} above threshold), T2map + T2part, {threads} threads; value = slab voxels / step time")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded 3-compartment EPG + Rician noise, 35% background)",
+        "config": config_dict(matrix, V, args.workload),
+        "method": "oracle: FP64 C restatement of the reference CPU path (Julia is not installed)",
+        "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": threads, "kind": "port", "sample": sample,
+                         "per_core": value / threads},
+        "e2e": {"value": value, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "published_reference": PUBLISHED.get(args.workload),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def profile_figure(name, key):
+    """A figure (per voxel) from a committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith(key + ":"):
+            return float(line.split(":")[1])
+    return None
+
+
+class DeviceRun:
+    """Device-resident inputs and outputs (torch owns the memory) and the
+    device-pointer C ABI call of one method.  f64: FP64 image and outputs
+    (the same values as the Float32 image, widened), for exact comparisons."""
+
+    OUT_KEYS = ["dist", "gdn", "ggm", "gva", "fnr", "snr", "alpha"]
+
+    def __init__(self, D, _lib, ctx, torch, mo, po, img, V, f64=False):
+        self.ctx, self.L, self.torch, self._lib = ctx, ctx.L, torch, _lib
+        n = mo.nT2
+        dt = torch.float64 if f64 else torch.float32
+        self.code = _lib.F64 if f64 else _lib.F32
+        self.stream = torch.cuda.current_stream()
+        h = img.reshape(-1, order="F")
+        self.d_img = torch.from_numpy(h.astype(np.float64) if f64 else h.copy()).cuda()
+        self.d_out = {"dist": torch.empty(V * n, dtype=dt, device="cuda")}
+        for k in self.OUT_KEYS[1:]:
+            self.d_out[k] = torch.empty(V, dtype=dt, device="cuda")
+        self.d_parts = {k: torch.empty(V, dtype=dt, device="cuda") for k in ("sfr", "sgm", "mfr", "mgm")}
+        self.mout = _lib.T2mapOutC(*[C.c_void_p(self.d_out[k].data_ptr()) if k in self.d_out else None
+                                     for k, _ in _lib.T2mapOutC._fields_])
+        self.pout = _lib.T2partOutC(*[C.c_void_p(self.d_parts[k].data_ptr()) for k, _ in _lib.T2partOutC._fields_])
+        self.mo_c, self.po_c = mo.to_c(), po.to_c()
+        self.V, self.n = V, n
+
+    def step(self):
+        self.ctx.check(self.L.decaes_t2map_t2part_device(
+            self.ctx.h, C.byref(self.mo_c), C.byref(self.po_c), C.c_void_p(self.d_img.data_ptr()), self.code, None,
+            C.byref(self.mout), C.byref(self.pout), C.c_void_p(self.stream.cuda_stream)))
+
+    def stats(self):
+        self.ctx.check(self.L.decaes_sync_stats(self.ctx.h, C.c_void_p(self.stream.cuda_stream)))
+        return self.ctx.stats()
+
+    def host(self):
+        """dist (V x nT2), alpha and sfr on the host, FP64."""
+        return (self.d_out["dist"].double().cpu().numpy().reshape(self.n, self.V).T,
+                self.d_out["alpha"].double().cpu().numpy(), self.d_parts["sfr"].double().cpu().numpy())
+
+    def timed(self, steps, warmup, world, clocks=None):
+        """W untimed steps, then K steps between barrier + synchronize; returns
+        (ms per step as the max over ranks, kernel launches, voxel-solve ms per step)."""
+        torch = self.torch
+        for _ in range(warmup):
+            self.step()
+        torch.cuda.synchronize()
+        self.stats()
+        replicas.barrier(world)
+        torch.cuda.synchronize()
+        solve_ms, launches = [], 0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with (clocks if clocks is not None else _Null()):
+            e0.record(self.stream)
+            for _ in range(steps):
+                self.step()
+                st = self.stats()
+                solve_ms.append(st["ms_solve"])
+                launches += st["kernel_launches"]
+            e1.record(self.stream)
+            torch.cuda.synchronize()
+        ms = replicas.max_over_ranks(e0.elapsed_time(e1), world, device="cuda")
+        replicas.barrier(world)
+        return ms / steps, launches, solve_ms
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+def dist_errors(d, ref):
+    """Per voxel (rows): the largest per-bin error |d - ref| / max(|ref|,
+    1e-12 sum|ref|) and the L1 error sum|d - ref| / sum|ref|."""
+    diff = np.abs(d - ref)
+    tot = np.abs(ref).sum(axis=1)
+    scale = np.maximum(np.abs(ref), 1e-12 * tot[:, None])
+    rel = np.where(scale > 0, diff / np.where(scale > 0, scale, 1), diff).max(axis=1)
+    l1 = np.where(tot > 0, diff.sum(axis=1) / np.where(tot > 0, tot, 1), diff.sum(axis=1))
+    return rel, l1
+
+
+def _q(x, q):
+    return float(np.quantile(x, q)) if x.size else 0.0
+
+
+def _mx(x):
+    return float(x.max()) if x.size else 0.0
+
+
+def method_errors(dist, alpha, sfr, rdist, ralpha, rsfr, tail=0):
+    """A method's per-output errors against reference outputs on the same
+    voxels (processed in the reference): MWF, distribution L1 and per-bin
+    relative error, flip angle; optionally the voxels with MWF error > 1e-3."""
+    ok = ~np.isnan(rsfr)
+    same = bool(np.array_equal(ok, ~np.isnan(sfr)))
+    dm = np.abs(sfr[ok] - rsfr[ok])
+    da = np.abs(alpha[ok] - ralpha[ok])
+    rel, l1 = dist_errors(dist[ok], rdist[ok])
+    out = {"voxels": int(ok.sum()), "same_processed_voxels": same,
+           "mwf_abs": {"max": _mx(dm), "p99": _q(dm, 0.99), "frac_gt_1e-3": float((dm > 1e-3).mean()) if dm.size else 0.0},
+           "dist_l1_rel": {"max": _mx(l1), "p99": _q(l1, 0.99)},
+           "dist_bin_rel": {"max": _mx(rel), "p99": _q(rel, 0.99)},
+           "alpha_abs_deg": {"max": _mx(da), "p99": _q(da, 0.99)}}
+    if tail:
+        idx = np.flatnonzero(ok)
+        big = np.argsort(-dm)[:tail]
+        out["largest_mwf_errors"] = [[int(idx[i]), float(dm[i])] for i in big if dm[i] > 1e-3]
+    return out
+
+
+def bitwise_frac(dist, alpha, sfr, rdist, ralpha, rsfr):
+    ok = ~np.isnan(rsfr)
+    eq = (dist[ok] == rdist[ok]).all(axis=1) & (alpha[ok] == ralpha[ok]) & (sfr[ok] == rsfr[ok])
+    return float(eq.mean()) if eq.size else 0.0
 
 
 class Clocks:
@@ -142,135 +380,6 @@ def fp64_peak_tflops(torch):
         best = min(best, e0.elapsed_time(e1))
     del a, b
     return 2 * n ** 3 / (best * 1e-3) / 1e12
-
-
-def cpu_baseline(mo, img_f32, sample, threads):
-    """The oracle (CPU restatement of the reference path) on a bounded sample of
-    above-threshold voxels; returns (voxels/s scaled to the whole image,
-    seconds, FP64 FLOPs per processed voxel)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    V = int(np.prod(mo.MatrixSize))
-    flat = img_f32.reshape((V, mo.nTE), order="F")
-    fg = np.flatnonzero(flat[:, 0] > mo.Threshold)
-    pick = fg[np.linspace(0, len(fg) - 1, min(sample, len(fg))).astype(np.int64)]
-    sub = flat[pick].astype(np.float64).reshape((len(pick), 1, 1, mo.nTE), order="F")
-    oo = O.T2mapOptions(MatrixSize=(len(pick), 1, 1), nTE=mo.nTE, TE=mo.TE, nT2=mo.nT2, T2Range=mo.T2Range,
-                        Reg=mo.Reg, nRefAngles=mo.nRefAngles, MinRefAngle=mo.MinRefAngle, Threshold=mo.Threshold,
-                        nRefAnglesMin=mo.nRefAnglesMin)
-    t0 = time.perf_counter()
-    maps, dist, fl = O.t2map(sub, oo, nthreads=threads, return_flops=True)
-    O.t2part(dist, O.T2partOptions(MatrixSize=(len(pick), 1, 1), nT2=mo.nT2, T2Range=mo.T2Range, SPWin=SPWIN,
-                                   MPWin=MPWIN))
-    dt = time.perf_counter() - t0
-    per_fg = dt / len(pick)
-    whole = per_fg * len(fg)  # projected time for the whole volume
-    return V / whole, dt, sum(fl.values()) / len(pick), len(pick), len(fg)
-
-
-def run_reference(args):
-    """Times the oracle (CPU restatement of the reference path) on host cores."""
-    import decaes_gb300 as D
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
-    matrix = tuple(args.matrix) if args.matrix else WORKLOADS[args.workload]["matrix"]
-    mo, po, mock = workload(matrix, "fp64", args.workload)
-    img = D.mock_image(mock, seed=args.seed, dtype=np.float32)
-    threads = os.cpu_count() or 1
-    sample = args.cpu_sample
-    for _ in range(args.warmup):
-        cpu_baseline(mo, img, max(64, sample // 16), threads)
-    vals = []
-    for _ in range(args.steps):
-        v, dt, flv, ns, nfg = cpu_baseline(mo, img, sample, threads)
-        vals.append(v)
-    V = int(np.prod(matrix))
-    value = statistics.median(vals)
-    line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": V / value * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded 3-compartment EPG + Rician noise, 35% background)",
-        "config": config_dict(matrix, "fp64", V, nfg, args.workload),
-        "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": threads, "kind": "port",
-                         "sample": f"{ns} above-threshold voxels per step (of {nfg}); time scaled to the whole volume"},
-        "e2e": {"value": value, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
-
-
-def profile_figure(name, key):
-    """A figure (per voxel) from a committed ncu summary, or None."""
-    p = os.path.join(ROOT, "profiles", name)
-    if not os.path.exists(p):
-        return None
-    for line in open(p):
-        if line.startswith(key + ":"):
-            return float(line.split(":")[1])
-    return None
-
-
-class DeviceRun:
-    """Device-resident inputs and outputs (torch owns the memory) and the
-    device-pointer C ABI call of one method."""
-
-    def __init__(self, D, _lib, ctx, torch, mo, po, img, V):
-        self.ctx, self.L, self.torch, self._lib = ctx, ctx.L, torch, _lib
-        n = mo.nT2
-        self.stream = torch.cuda.current_stream()
-        self.d_img = torch.from_numpy(img.reshape(-1, order="F").copy()).cuda()
-        keys = ["dist", "gdn", "ggm", "gva", "fnr", "snr", "alpha"]
-        self.d_out = {"dist": torch.empty(V * n, dtype=torch.float32, device="cuda")}
-        for k in keys[1:]:
-            self.d_out[k] = torch.empty(V, dtype=torch.float32, device="cuda")
-        self.d_parts = {k: torch.empty(V, dtype=torch.float32, device="cuda") for k in ("sfr", "sgm", "mfr", "mgm")}
-        self.mout = _lib.T2mapOutC(*[C.c_void_p(self.d_out[k].data_ptr()) if k in self.d_out else None
-                                     for k, _ in _lib.T2mapOutC._fields_])
-        self.pout = _lib.T2partOutC(*[C.c_void_p(self.d_parts[k].data_ptr()) for k, _ in _lib.T2partOutC._fields_])
-        self.mo_c, self.po_c = mo.to_c(), po.to_c()
-
-    def step(self):
-        self.ctx.check(self.L.decaes_t2map_t2part_device(
-            self.ctx.h, C.byref(self.mo_c), C.byref(self.po_c), C.c_void_p(self.d_img.data_ptr()), self._lib.F32, None,
-            C.byref(self.mout), C.byref(self.pout), C.c_void_p(self.stream.cuda_stream)))
-
-    def stats(self):
-        self.ctx.check(self.L.decaes_sync_stats(self.ctx.h, C.c_void_p(self.stream.cuda_stream)))
-        return self.ctx.stats()
-
-    def timed(self, steps, warmup, world, clocks=None):
-        """W untimed steps, then K steps between barrier + synchronize; returns
-        (ms per step as the max over ranks, kernel launches, voxel-solve ms per step)."""
-        torch = self.torch
-        for _ in range(warmup):
-            self.step()
-        torch.cuda.synchronize()
-        self.stats()
-        replicas.barrier(world)
-        torch.cuda.synchronize()
-        solve_ms, launches = [], 0
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with (clocks if clocks is not None else _Null()):
-            e0.record(self.stream)
-            for _ in range(steps):
-                self.step()
-                st = self.stats()
-                solve_ms.append(st["ms_solve"])
-                launches += st["kernel_launches"]
-            e1.record(self.stream)
-            torch.cuda.synchronize()
-        ms = replicas.max_over_ranks(e0.elapsed_time(e1), world, device="cuda")
-        replicas.barrier(world)
-        return ms / steps, launches, solve_ms
-
-
-class _Null:
-    def __enter__(self):
-        return self
-
-    def __exit__(self, *a):
-        return False
 
 
 def run_batch_workload(args):
@@ -441,21 +550,24 @@ def main():
     ap.add_argument("--no-fp64-compare", action="store_true",
                     help="skip the FP64 comparison run of the mixed headline")
     ap.add_argument("--workload", default="lcurve48", choices=sorted(WORKLOADS) + ["batch", "serve"],
-                    help="lcurve48 (headline), gcv56, batch (uneven volumes in one launch), serve (serving mix)")
+                    help="lcurve48 (headline), gcv56, chi2k8_48, batch (uneven volumes in one launch), serve")
     ap.add_argument("--nvol", type=int, default=256, help="volumes of --workload batch")
     ap.add_argument("--rates", default="0.5,1,2", help="arrival rates (requests/s) of --workload serve")
     ap.add_argument("--requests", type=int, default=40, help="requests per rate of --workload serve")
     ap.add_argument("--tick-voxels", type=int, default=262144, help="voxels per server tick (--workload serve)")
     ap.add_argument("--matrix", type=int, nargs=3, default=None, help="override the workload's MatrixSize")
     ap.add_argument("--compare-slices", type=int, default=None,
-                    help="z-slices of the volume the FP64 comparison runs on (default: all for lcurve48, 2 for gcv56)")
+                    help="z-slices of the volume the FP64 comparison runs on (default: all for the 48-echo "
+                         "workloads, 8 for gcv56)")
+    ap.add_argument("--ref-slices", type=int, default=None,
+                    help="z-slices of the volume one --impl reference step runs on")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-sample", type=int, default=None,
-                    help="above-threshold voxels the CPU oracle times (default ~10-20 s of 16-core work)")
+                    help="above-threshold voxels the CPU oracle runs on for cpu_baseline and parity")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.cpu_sample is None:
-        args.cpu_sample = 131072 if args.workload == "lcurve48" else 16384
+        args.cpu_sample = {"lcurve48": 131072, "chi2k8_48": 131072}.get(args.workload, 16384)
     if args.impl == "reference":
         if args.workload in ("batch", "serve"):
             print(json.dumps({"impl": "reference", "unavailable": "the batched workload is this library's own "
@@ -489,7 +601,7 @@ def main():
     ms_per_step, launches, solve_ms = run.timed(args.steps, args.warmup, world, clk)
     Vp = run.stats()["voxels_processed"]
     value = replicas.aggregate_voxels_per_s(V, ms_per_step, world)
-    sfr_head = run.d_parts["sfr"].double().cpu().numpy()
+    head = run.host()
 
     # ---- end to end through the host-buffer C ABI from pinned memory ----
     mo_c, po_c = run.mo_c, run.po_c
@@ -498,41 +610,36 @@ def main():
     h_parts = {k: torch.empty_like(v, device="cpu").pin_memory() for k, v in run.d_parts.items()}
     hm = _lib.T2mapOutC(*[C.c_void_p(h_out[k].data_ptr()) if k in h_out else None for k, _ in _lib.T2mapOutC._fields_])
     hp = _lib.T2partOutC(*[C.c_void_p(h_parts[k].data_ptr()) for k, _ in _lib.T2partOutC._fields_])
+    del run
     torch.cuda.synchronize()
+    replicas.barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         ctx.check(ctx.L.decaes_t2map_t2part(ctx.h, C.byref(mo_c), C.byref(po_c), C.c_void_p(h_img.data_ptr()),
                                             _lib.F32, None, C.byref(hm), C.byref(hp)))
-    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_s = replicas.max_over_ranks((time.perf_counter() - t0) / args.steps, world, device="cuda")
     h2d = img.nbytes
     d2h = sum(v.numel() * 4 for v in h_out.values()) + sum(v.numel() * 4 for v in h_parts.values())
+    del h_out, h_parts, h_img
 
-    # ---- the FP64 method on the same volume: throughput and the MWF gate ----
-    compare = None
-    if args.precision == "mixed" and not args.no_fp64_compare:
-        nz = args.compare_slices or (matrix[2] if args.workload == "lcurve48" else min(2, matrix[2]))
-        nz = max(1, min(nz, matrix[2]))
+    # ---- the FP64 method on the volume (or its leading slices), FP64 outputs ----
+    flat = img.reshape((V, -1), order="F")
+    nz = matrix[2]
+    if args.workload == "gcv56":
+        nz = 8
+    if args.compare_slices:
+        nz = args.compare_slices
+    nz = max(1, min(nz, matrix[2]))
+    Vs = matrix[0] * matrix[1] * nz
+    fp64 = None
+    ms64 = None
+    if not args.no_fp64_compare:
         sub = (matrix[0], matrix[1], nz)
-        Vs = int(np.prod(sub))
-        img_s = np.ascontiguousarray(img.reshape((V, -1), order="F")[:Vs]).reshape((*sub, -1), order="F")
+        img_s = np.ascontiguousarray(flat[:Vs]).reshape((*sub, -1), order="F")
         mo64, po64, _ = workload(sub, "fp64", args.workload)
-        run64 = DeviceRun(D, _lib, ctx, torch, mo64, po64, img_s, Vs)
-        ms64, _, _ = run64.timed(1, 1, world)
-        sfr64 = run64.d_parts["sfr"].double().cpu().numpy()
-        head_s = sfr_head[:Vs]
-        ok = ~np.isnan(sfr64)
-        same_mask = bool(np.array_equal(ok, ~np.isnan(head_s)))
-        d = np.abs(head_s[ok] - sfr64[ok])
-        compare = {
-            "fp64_value": world * Vs / (ms64 * 1e-3), "fp64_ms_per_step": ms64,
-            "fp64_volume": f"{sub[0]}x{sub[1]}x{sub[2]} (first {nz} of {matrix[2]} z-slices)",
-            "speedup_vs_fp64": (world * V / (ms_per_step * 1e-3)) / (world * Vs / (ms64 * 1e-3)),
-            "mwf_abs_err_vs_fp64": {"max": float(d.max()), "p99": float(np.quantile(d, 0.99)),
-                                    "frac_gt_1e-3": float(np.mean(d > 1e-3)), "voxels": int(ok.sum()),
-                                    "same_processed_voxels": same_mask},
-            "gate": "MWF |mixed - FP64| p99 <= 1e-3 over every processed voxel of the volume",
-            "gate_met": bool(np.quantile(d, 0.99) <= 1e-3 and same_mask),
-        }
+        run64 = DeviceRun(D, _lib, ctx, torch, mo64, po64, img_s, Vs, f64=True)
+        ms64, _, _ = run64.timed(1, 0, world)
+        fp64 = run64.host()
         del run64
 
     if rank != 0:
@@ -542,33 +649,70 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
         "data": "synthetic (seeded 3-compartment EPG + Rician noise, 35% background)",
-        "config": config_dict(matrix, args.precision, V, Vp, args.workload),
+        "config": config_dict(matrix, V, args.workload),
+        "method": args.precision,
+        "voxels_above_threshold": Vp,
+        "voxels_above_threshold_per_s": world * Vp / (ms_per_step * 1e-3),
         "e2e": {"value": world * V / e2e_s, "unit": "voxels/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
-    # above-threshold voxels per second (rank 0's count times the ranks)
-    line["config"]["voxels_above_threshold_per_s"] = world * Vp / (ms_per_step * 1e-3)
-    if compare is not None:
-        line["mixed_vs_fp64"] = compare
-    # ---- roofline of the voxel-solve kernel and the CPU baseline ----
+    pub = PUBLISHED.get(args.workload)
+    if pub:
+        line["published_reference"] = dict(pub, e2e_ratio=line["e2e"]["value"] / pub["value"],
+                                           value_ratio=value / pub["value"])
+    if ms64 is not None and args.precision == "mixed":
+        hs = tuple(a[:Vs] for a in head)
+        line["mixed_vs_fp64"] = {
+            "fp64_value": world * Vs / (ms64 * 1e-3), "fp64_ms_per_step": ms64,
+            "fp64_volume": f"{matrix[0]}x{matrix[1]}x{nz} (first {nz} of {matrix[2]} z-slices), FP64 image and outputs",
+            "speedup_vs_fp64": (world * V / (ms_per_step * 1e-3)) / (world * Vs / (ms64 * 1e-3)),
+            "errors": method_errors(*hs, *fp64, tail=32),
+            "gate": "MWF |mixed - FP64| p99 <= 1e-3 over every processed voxel of the compared volume",
+        }
+        e = line["mixed_vs_fp64"]["errors"]
+        line["mixed_vs_fp64"]["gate_met"] = bool(e["mwf_abs"]["p99"] <= 1e-3 and e["same_processed_voxels"])
+
+    # ---- the oracle on a sample: CPU baseline and parity at this scale ----
     peak = fp64_peak_tflops(torch)
     kern_ms = statistics.median(solve_ms)
-    cv = None
+    cb = None
     if not args.no_cpu_baseline:
-        cv, cdt, flops_per_voxel, ns, nfg = cpu_baseline(mo, img, args.cpu_sample, os.cpu_count() or 1)
-        line["cpu_baseline"] = {"value": cv, "unit": "voxels/s", "cores": os.cpu_count() or 1, "kind": "port",
-                                "sample": f"{ns} above-threshold voxels of the same image ({cdt:.1f} s, FP64 "
-                                          f"restatement of the reference path); time scaled to the whole volume"}
+        threads = os.cpu_count() or 1
+        # the sample is drawn from the voxels the FP64 comparison covers
+        Vp_s = int((flat[:Vs, 0] > THRESHOLD).sum())
+        cb = cpu_baseline(args.workload, flat[:Vs], Vp_s, args.cpu_sample, threads)
+        line["cpu_baseline"] = {"value": cb["value"], "unit": "voxels/s", "cores": threads, "kind": "port",
+                                "per_core": cb["value"] / threads,
+                                "sample": f"{len(cb['pick'])} above-threshold voxels of the same image "
+                                          f"({cb['seconds']:.1f} s, FP64 restatement of the reference path); "
+                                          f"time per voxel scaled to the whole volume"}
+        pk = cb["pick"]
+        o_d, o_a, o_s = cb["dist"], cb["maps"]["alpha"], cb["parts"]["sfr"]
+        par = {"sample_voxels": int(len(pk)), "oracle": "FP64 C restatement of the reference path (oracle/)"}
+        if fp64 is not None:
+            d64, a64, s64 = (x[pk] for x in fp64)
+            e64 = method_errors(d64, a64, s64, o_d, o_a, o_s)
+            par["fp64_vs_oracle"] = {
+                "bitwise_frac": bitwise_frac(d64, a64, s64, o_d, o_a, o_s), **e64,
+                "gate": "per-bin relative <= 1e-8 and |MWF| <= 1e-10",
+                "gate_met": bool(e64["dist_bin_rel"]["max"] <= 1e-8 and e64["mwf_abs"]["max"] <= 1e-10
+                                 and e64["same_processed_voxels"])}
+        if args.precision == "mixed":
+            dm, am, sm = (x[pk] for x in head)
+            em = method_errors(dm, am, sm, o_d, o_a, o_s)
+            par["mixed_vs_oracle"] = {**em, "gate": "MWF |mixed - oracle| p99 <= 1e-3",
+                                      "gate_met": bool(em["mwf_abs"]["p99"] <= 1e-3 and em["same_processed_voxels"])}
+        line["parity"] = par
     if args.precision == "fp64":
-        if cv is not None:
-            achieved = flops_per_voxel * Vp / (kern_ms * 1e-3) / 1e12
+        if cb is not None:
+            achieved = cb["flops_per_voxel"] * Vp / (kern_ms * 1e-3) / 1e12
             tpv = profile_figure(f"k_voxels_fp64_{args.workload}.md", "dram_bytes_per_voxel")  # ncu on a small slab
             line["roofline"] = {"kernel": "k_voxels_plain (FP64 method)", "bound": "fp64", "achieved": achieved,
                                 "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                                 "traffic": None if tpv is None else tpv * Vp,
-                                "work": f"{flops_per_voxel / 1e6:.3f} MFLOP FP64 per above-threshold voxel "
+                                "work": f"{cb['flops_per_voxel'] / 1e6:.3f} MFLOP FP64 per above-threshold voxel "
                                         f"(the reference algorithm, counted by the oracle) x {Vp} voxels",
                                 "kernel_ms": kern_ms,
                                 "peak_source": "cuBLAS DGEMM (torch.matmul float64 4096^3) measured in this run"}
@@ -584,6 +728,12 @@ def main():
                                         f"mixed method, ncu thread-instruction counts, FMA = 2) x {Vp} voxels",
                                 "kernel_ms": kern_ms,
                                 "peak_source": "cuBLAS DGEMM (torch.matmul float64 4096^3) measured in this run"}
+            if cb is not None:
+                alg = cb["flops_per_voxel"] * Vp / (kern_ms * 1e-3) / 1e12
+                line["roofline"]["reference_algorithm_view"] = {
+                    "achieved": alg, "frac": alg / peak, "unit": "TFLOP/s",
+                    "work": f"{cb['flops_per_voxel'] / 1e6:.3f} MFLOP FP64 per voxel: the reference algorithm's "
+                            f"operations (oracle-counted), which the mixed method replaces by fewer"}
     if "roofline" in line:
         line["roofline"]["hbm_view"] = hbm_view(mo, Vp, V, kern_ms)
     print(json.dumps(line), flush=True)

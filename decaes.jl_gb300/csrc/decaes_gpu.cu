@@ -205,6 +205,22 @@ __global__ void k_narrow(const double *src, float *dst, long len) {
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
+namespace dh {
+// One lock for every change of a kernel's dynamic shared-memory limit in the
+// library (the context paths and the no-allocation entry point).  The limit is
+// only ever raised: a launch planned for a size below it stays valid whatever
+// another thread or context sets in between.
+int raise_smem_limit(const void *kern, size_t bytes) {
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, kern);
+    if (e != cudaSuccess) return (int)e;
+    if ((size_t)a.maxDynamicSharedSizeBytes >= bytes) return (int)cudaSuccess;
+    return (int)cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+}  // namespace dh
+
 namespace {
 
 struct DevBuf {
@@ -464,7 +480,7 @@ int most_warps_wpb(decaes_ctx *ctx, Kern kern, long stride, int max_wpb) {
     for (int w = 1; w <= max_wpb; ++w) {
         const size_t smem = (size_t)w * stride * sizeof(double);
         if (smem > ctx->smem_optin) break;
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) break;
+        if (dh::raise_smem_limit((const void *)kern, smem) != (int)cudaSuccess) break;
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * w, smem) != cudaSuccess) break;
         if (per_sm * w > best_warps) { best_warps = per_sm * w; best = w; }
@@ -479,7 +495,7 @@ int launch_shape(decaes_ctx *ctx, Kern kern, long stride, int *wpb, int *grid, s
     for (; *wpb >= 1; *wpb >>= 1) {
         *smem = (size_t)*wpb * stride * sizeof(double);
         if (*smem > ctx->smem_optin) continue;
-        CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem));
+        CK((cudaError_t)dh::raise_smem_limit((const void *)kern, *smem));
         int per_sm = 0;
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * *wpb, *smem));
         if (per_sm >= 1) {
@@ -797,6 +813,13 @@ extern "C" int decaes_t2map_t2part_device(decaes_ctx *ctx, const decaes_t2map_op
         {om.sfr, d_pout ? d_pout->sfr : nullptr, (size_t)V}, {om.sgm, d_pout ? d_pout->sgm : nullptr, (size_t)V},
         {om.mfr, d_pout ? d_pout->mfr : nullptr, (size_t)V}, {om.mgm, d_pout ? d_pout->mgm : nullptr, (size_t)V},
     };
+    // with SetFlipAngle the saved basis is the one nTE x nT2 basis of the volume
+    const double *fixed_basis = nullptr;
+    if (!std::isnan(o.SetFlipAngle) && o.SaveNNLSBasis && d_mout->decaybasis) {
+        Basis *B;
+        if (int rc = get_basis(ctx, o, &B)) return rc;
+        fixed_basis = B->fixed;
+    }
     for (auto &c : cp) {
         if (!c.s || !c.d) continue;
         if (dtype == DECAES_F64) {
@@ -804,6 +827,14 @@ extern "C" int decaes_t2map_t2part_device(decaes_ctx *ctx, const decaes_t2map_op
         } else {
             int g = (int)std::min<long>(8L * ctx->sms, ((long)c.len + 255) / 256);
             dk::k_narrow<<<std::max(g, 1), 256, 0, st>>>(c.s, (float *)c.d, (long)c.len);
+            ++launches;
+        }
+    }
+    if (fixed_basis) {
+        if (dtype == DECAES_F64) {
+            CK(cudaMemcpyAsync(d_mout->decaybasis, fixed_basis, sizeof(double) * m * n, cudaMemcpyDeviceToDevice, st));
+        } else {
+            dk::k_narrow<<<(int)((m * n + 255) / 256), 256, 0, st>>>(fixed_basis, (float *)d_mout->decaybasis, (long)(m * n));
             ++launches;
         }
     }

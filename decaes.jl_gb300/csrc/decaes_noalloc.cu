@@ -14,6 +14,7 @@
 // The kernels are the ones of the context path (decaes_gpu.cu), given
 // addresses inside the static array instead of cudaMalloc'ed buffers, so the
 // results are bit-identical to decaes_t2map_t2part_device.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -52,6 +53,7 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_workspace[kStaticBytes];
 
 struct DeviceSetup {
+    unsigned long long ctx_id = 0;  // context the address was looked up in (0: none cached)
     unsigned char *base = nullptr;
     int sms = 0;
     int smem_optin = 0;
@@ -68,26 +70,69 @@ int fail(char *err, size_t errlen, int code, const std::string &msg) {
     return code;
 }
 
-// Once per device, with that device current: look up the array's address (the
-// lookup also loads this module, which is when the array is reserved) and the
-// device's SM count and shared-memory limit.
+// Identity of the calling thread's current CUDA context: unique for every
+// context the process creates, so it changes when the primary context is
+// re-created after cudaDeviceReset and differs between driver-API contexts
+// on one device.  0 when there is no current context or the driver does not
+// provide the query.  The driver functions are reached through the runtime's
+// entry-point lookup, so the library does not link libcuda itself.
+unsigned long long current_context_id() {
+    using GetCurrent = CUresult (*)(CUcontext *);
+    using GetId = CUresult (*)(CUcontext, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {  // g_mu is held
+        looked_up = true;
+        void *p = nullptr, *q = nullptr;
+        cudaDriverEntryPointQueryResult r1 = cudaDriverEntryPointSymbolNotFound, r2 = r1;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &r1) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &q, 12000, cudaEnableDefault, &r2) == cudaSuccess &&
+            r1 == cudaDriverEntryPointSuccess && r2 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<GetCurrent>(p);
+            get_id = reinterpret_cast<GetId>(q);
+        }
+        cudaGetLastError();  // a failed lookup leaves no sticky error behind
+    }
+    if (!get_current || !get_id) return 0;
+    CUcontext c = nullptr;
+    if (get_current(&c) != CUDA_SUCCESS || !c) return 0;
+    unsigned long long id = 0;
+    if (get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Set-up, with the device current: look up the array's address (the lookup
+// also loads this module in the current context, which is when the array is
+// reserved) and the device's SM count and shared-memory limit.  The address
+// belongs to the context it was looked up in, so it is cached per device
+// together with that context's identity and looked up again whenever the
+// current context differs (after cudaDeviceReset, or under another
+// driver-API context).  Without a context identity nothing is cached and the
+// lookup runs on every call.
 int setup_device(int dev, DeviceSetup *out, char *err, size_t errlen) {
     if (dev < 0 || dev >= kMaxDevices) return fail(err, errlen, DECAES_EINVAL, "device ordinal out of range");
     std::lock_guard<std::mutex> lk(g_mu);
     DeviceSetup &s = g_setup[dev];
-    if (!s.base) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_workspace);
-        if (e != cudaSuccess) return fail(err, errlen, DECAES_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        int sms = 0, optin = 0;
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        if (e != cudaSuccess) return fail(err, errlen, DECAES_ECUDA, std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e));
-        s.sms = sms;
-        s.smem_optin = optin;
-        s.base = static_cast<unsigned char *>(p);
+    const unsigned long long id = current_context_id();
+    if (id != 0 && s.base && s.ctx_id == id) {
+        *out = s;
+        return DECAES_OK;
     }
-    *out = s;
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_workspace);
+    if (e != cudaSuccess) return fail(err, errlen, DECAES_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    int sms = 0, optin = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return fail(err, errlen, DECAES_ECUDA, std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e));
+    DeviceSetup fresh;
+    fresh.base = static_cast<unsigned char *>(p);
+    fresh.sms = sms;
+    fresh.smem_optin = optin;
+    fresh.ctx_id = current_context_id();  // the lookup made the device's context current if none was
+    s = fresh.ctx_id ? fresh : DeviceSetup{};
+    *out = fresh;
     return DECAES_OK;
 }
 
@@ -142,6 +187,16 @@ extern "C" int decaes_t2map_t2part_noalloc(const decaes_t2map_opts *mopts, const
                     "echotimes, t2times, refangleset and decaybasisset are not written by this entry point; pass NULL");
     if (d_pout && (!d_pout->sfr || !d_pout->sgm || !d_pout->mfr || !d_pout->mgm))
         return fail(err, errlen, DECAES_EINVAL, "sfr, sgm, mfr and mgm outputs are required with T2part options");
+    // Optional outputs follow their Save* flags, as the other entry points do;
+    // a buffer whose flag is off would never be written, so it is refused.
+    if (out.resnorm && !o.SaveResidualNorm)
+        return fail(err, errlen, DECAES_EINVAL, "resnorm is written only with SaveResidualNorm; pass NULL or set the flag");
+    if (out.decaycurve && !o.SaveDecayCurve)
+        return fail(err, errlen, DECAES_EINVAL, "decaycurve is written only with SaveDecayCurve; pass NULL or set the flag");
+    if ((out.mu || out.chi2factor) && !o.SaveRegParam)
+        return fail(err, errlen, DECAES_EINVAL, "mu and chi2factor are written only with SaveRegParam; pass NULL or set the flag");
+    if (out.decaybasis && !o.SaveNNLSBasis)
+        return fail(err, errlen, DECAES_EINVAL, "decaybasis is written only with SaveNNLSBasis; pass NULL or set the flag");
 
     if (o.precision != DECAES_PREC_FP64)
         return fail(err, errlen, DECAES_EINVAL, "this entry point runs the FP64 method only (precision = DECAES_PREC_FP64)");
@@ -185,7 +240,7 @@ extern "C" int decaes_t2map_t2part_noalloc(const decaes_t2map_opts *mopts, const
                         "-byte static workspace (grows with the voxel count, nTE*nT2*nRefAngles and nT2); "
                         "split the image into smaller slabs");
     auto kern = o.legacy ? dk::k_voxels_legacy : dk::k_voxels_plain;
-    NA_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NA_CK((cudaError_t)dh::raise_smem_limit((const void *)kern, smem));
     int per_sm = 0;
     NA_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem));
     if (per_sm < 1) return fail(err, errlen, DECAES_EINVAL, "voxel kernel cannot be resident with this workspace size");

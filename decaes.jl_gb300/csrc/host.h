@@ -23,4 +23,9 @@ std::string t2part_plan(const decaes_t2part_opts &o, T2partPlan &p);
 
 int mock_image(const decaes_mock_opts &o, uint64_t seed, void *image, int dtype, int nthreads);
 
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` on the
+// current device, never lowering it; returns the cudaError_t value (defined
+// in decaes_gpu.cu).
+int raise_smem_limit(const void *kern, size_t bytes);
+
 }  // namespace dh

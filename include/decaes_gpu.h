@@ -264,8 +264,12 @@ void decaes_server_destroy(decaes_server *srv);
  * All pointers are device addresses on the CURRENT device; `stream` is a
  * cudaStream_t (NULL = the legacy default stream).  `d_image` (and the optional
  * `d_b1map`) are DECAES_F32 or DECAES_F64 per `dtype`; every output is FP64
- * whatever `dtype` is.  dist, gdn, ggm, gva, fnr, snr and alpha are required;
- * resnorm, decaycurve, mu, chi2factor and decaybasis are written when non-NULL;
+ * whatever `dtype` is.  dist, gdn, ggm, gva, fnr, snr and alpha are required.
+ * The optional outputs follow their Save* flags as in the other entry points:
+ * resnorm (SaveResidualNorm), decaycurve (SaveDecayCurve), mu and chi2factor
+ * (SaveRegParam), decaybasis (SaveNNLSBasis: V x nTE x nT2, or nTE x nT2 with
+ * SetFlipAngle); a non-NULL optional buffer whose flag is off is refused with
+ * DECAES_EINVAL, a NULL one whose flag is on is simply not written.
  * echotimes, t2times, refangleset and decaybasisset must be NULL.  T2part is
  * fused when `popts` and `d_pout` are given (both or neither).  The library
  * NaN-fills the outputs before the solve.  Returns before the work finishes:
@@ -280,11 +284,14 @@ void decaes_server_destroy(decaes_server *srv);
  * scratch; a problem whose fixed part leaves no room for one warp's scratch is
  * rejected with DECAES_ENOMEM (split the image into slabs: voxels are
  * independent).  Fewer resident warps fit when the voxel list is large, which
- * lowers throughput but not the results, which are bit-identical to
- * decaes_t2map_t2part_device.
+ * lowers throughput but not the results, which are bit-identical to the FP64
+ * outputs of decaes_t2map_t2part_device (for a DECAES_F32 call that entry
+ * point returns these values rounded to float).
  *
- * The first call on each device does a one-time set-up (symbol lookup of the
- * array, device attributes); make that first call before any stream capture.
+ * The first call on a device does a set-up (symbol lookup of the array in the
+ * current context, device attributes), and so does the first call after the
+ * device's current context changes (cudaDeviceReset, or another driver-API
+ * context made current); make such a call before any stream capture.
  * All calls on a device share the array and it keeps the last call's contents:
  * calls that overlap in time on one device -- from two host threads or on two
  * streams -- race on it and give undefined results.  Serialize them. */

@@ -2529,3 +2529,102 @@ double orc_lcurve_corner(orc_fn2 f, void *ctx, double xlow, double xhigh, double
     free(r.fc_x); free(r.fc_P); free(r.pc_x); free(r.pc_P); free(r.pc_C); free(r.sc_x); free(r.sc_P);
     return x;
 }
+
+
+/* ==========================================================================
+ * Synthetic multi-echo image (test and benchmark input, not part of the
+ * reference path): per voxel three constant-flip EPG decays (myelin,
+ * intra/extracellular, CSF) at one refocusing angle, mixed, scaled and given
+ * Rician noise.  The reference's own generator (mock_image,
+ * src/utils.jl:606-668) draws bi-exponential decays; this one is the
+ * generator of the benchmark configurations and produces exactly the bytes
+ * of libdecaes_gpu's decaes_mock_image, so the CPU baseline can make its
+ * input without loading the GPU library.  Counter-based: voxel v draws from
+ * a xoshiro256** stream seeded by splitmix64 from (seed, v), so any slab of
+ * the volume can be generated on its own and thread count does not matter.
+ * ========================================================================== */
+typedef struct { uint64_t s[4]; } orc_rng;
+static uint64_t orc_splitmix(uint64_t *x) {
+    uint64_t z = (*x += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+static void orc_rng_init(orc_rng *g, uint64_t seed, uint64_t stream) {
+    uint64_t x = seed ^ (stream * 0xd1b54a32d192ed03ull);
+    for (int i = 0; i < 4; ++i) g->s[i] = orc_splitmix(&x);
+}
+static uint64_t orc_rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+static uint64_t orc_rng_next(orc_rng *g) {
+    uint64_t *s = g->s;
+    uint64_t r = orc_rotl(s[1] * 5, 7) * 9, t = s[1] << 17;
+    s[2] ^= s[0]; s[3] ^= s[1]; s[1] ^= s[2]; s[0] ^= s[3]; s[2] ^= t; s[3] = orc_rotl(s[3], 45);
+    return r;
+}
+static double orc_unif(orc_rng *g) { return (double)(orc_rng_next(g) >> 11) * 0x1.0p-53; }
+static double orc_unif_in(orc_rng *g, const double *r) { return r[0] + (r[1] - r[0]) * orc_unif(g); }
+static double orc_normal(orc_rng *g) { /* Box-Muller */
+    double u1 = orc_unif(g), u2 = orc_unif(g);
+    if (u1 < 1e-300) u1 = 1e-300;
+    return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+typedef struct {
+    const orc_mock_opts *o;
+    uint64_t seed;
+    long V, v0, v1;
+    void *image;
+    int f32;
+} mock_job;
+
+static void *mock_worker(void *arg) {
+    const mock_job *J = (const mock_job *)arg;
+    const orc_mock_opts *o = J->o;
+    const int m = o->nTE;
+    double *d1 = (double *)malloc(sizeof(double) * 3 * (size_t)m), *d2 = d1 + m, *d3 = d2 + m;
+    for (long v = J->v0; v < J->v1; ++v) {
+        orc_rng g;
+        orc_rng_init(&g, J->seed, (uint64_t)v);
+        double alpha = orc_unif_in(&g, o->FlipAngleRange);
+        double wmy = orc_unif_in(&g, o->MyelinFracRange), t2my = orc_unif_in(&g, o->MyelinT2Range);
+        double t2ie = orc_unif_in(&g, o->IET2Range);
+        double wcsf = orc_unif_in(&g, o->CSFFracRange), t2csf = orc_unif_in(&g, o->CSFT2Range);
+        double amp = orc_unif_in(&g, o->AmplitudeRange), snr = orc_unif_in(&g, o->SNRRange);
+        int bg = orc_unif(&g) < o->BackgroundFraction;
+        double wie = 1.0 - wmy - wcsf;
+        orc_epg_decay_curve(m, alpha, o->TE, t2my, o->T1, 180.0, d1);
+        orc_epg_decay_curve(m, alpha, o->TE, t2ie, o->T1, 180.0, d2);
+        orc_epg_decay_curve(m, alpha, o->TE, t2csf, o->T1, 180.0, d3);
+        double sigma = bg ? o->BackgroundSigma : amp / snr;
+        for (int e = 0; e < m; ++e) {
+            double sig = bg ? 0.0 : amp * (wmy * d1[e] + wie * d2[e] + wcsf * d3[e]);
+            double zr = orc_normal(&g), zi = orc_normal(&g);
+            double val = sqrt((sig + sigma * zr) * (sig + sigma * zr) + (sigma * zi) * (sigma * zi));
+            if (J->f32) ((float *)J->image)[v + J->V * e] = (float)val;
+            else ((double *)J->image)[v + J->V * e] = val;
+        }
+    }
+    free(d1);
+    return NULL;
+}
+
+int orc_mock_image(const orc_mock_opts *o, uint64_t seed, long V, void *image, int f32, int nthreads) {
+    if (!o || !image || V <= 0 || o->nTE < 1) return 1;
+    if (nthreads < 1) nthreads = 1;
+    mock_job *jobs = (mock_job *)malloc(sizeof(mock_job) * nthreads);
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+    long chunk = (V + nthreads - 1) / nthreads;
+    int nt = 0;
+    for (int t = 0; t < nthreads; ++t) {
+        long a = t * chunk, b = a + chunk < V ? a + chunk : V;
+        if (a >= b) break;
+        mock_job J = {o, seed, V, a, b, image, f32};
+        jobs[nt] = J;
+        pthread_create(&th[nt], NULL, mock_worker, &jobs[nt]);
+        ++nt;
+    }
+    for (int t = 0; t < nt; ++t) pthread_join(th[t], NULL);
+    free(jobs);
+    free(th);
+    return 0;
+}

@@ -20,6 +20,7 @@
 #define DECAES_ORACLE_H
 
 #include <stddef.h>
+#include <stdint.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -85,6 +86,26 @@ enum {
 int orc_t2map(const orc_t2map_opts *o, const double *image, long V, const double *b1map,
               orc_t2map_out *out, int nthreads, double *flops /* ORC_NSTAGES or NULL */);
 int orc_t2part(const orc_t2part_opts *o, const double *dist, long V, orc_t2part_out *out, int nthreads);
+
+/* ---- synthetic benchmark image (the same bytes as decaes_mock_image) ---- */
+typedef struct {
+    int nTE;
+    double TE;
+    double T1;
+    double FlipAngleRange[2];   /* degrees, uniform */
+    double MyelinT2Range[2];    /* seconds */
+    double MyelinFracRange[2];
+    double IET2Range[2];
+    double CSFT2Range[2];
+    double CSFFracRange[2];
+    double AmplitudeRange[2];
+    double SNRRange[2];         /* linear SNR; noise sigma = amplitude / SNR */
+    double BackgroundFraction;  /* voxels with zero amplitude (noise only) */
+    double BackgroundSigma;
+} orc_mock_opts;
+/* image[v + V*e] for voxels 0..V-1 (a leading slab of a larger volume is the
+ * same bytes as that volume's first V voxels); f32 != 0 writes floats. */
+int orc_mock_image(const orc_mock_opts *o, uint64_t seed, long V, void *image, int f32, int nthreads);
 
 /* ---- grids ---- */
 void orc_linrange(double a, double b, int len, double *out);

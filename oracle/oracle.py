@@ -56,6 +56,13 @@ FN = C.CFUNCTYPE(C.c_double, C.c_double, C.c_void_p)
 FN2 = C.CFUNCTYPE(None, C.c_double, _dp, C.c_void_p)
 
 
+class _MockOpts(C.Structure):
+    _fields_ = [("nTE", C.c_int), ("TE", C.c_double), ("T1", C.c_double)] + [
+        (k, C.c_double * 2) for k in ("FlipAngleRange", "MyelinT2Range", "MyelinFracRange", "IET2Range", "CSFT2Range",
+                                     "CSFFracRange", "AmplitudeRange", "SNRRange")] + [
+        ("BackgroundFraction", C.c_double), ("BackgroundSigma", C.c_double)]
+
+
 def build(force: bool = False) -> str:
     """Compile liboracle.so with the Makefile beside this file."""
     src = os.path.join(_HERE, "decaes_oracle.c")
@@ -101,6 +108,7 @@ def lib():
         L.orc_fitpack_splev.argtypes = [_dp, C.c_int, _dp, C.c_int, _dp, C.c_int, _dp]
         L.orc_spline_opt_legacy.argtypes = [_dp, _dp, C.c_int, _dp, _dp]
         L.orc_spline_root_legacy.argtypes = [_dp, _dp, C.c_int, C.c_double, _dp]
+        L.orc_mock_image.argtypes = [C.POINTER(_MockOpts), C.c_uint64, C.c_long, C.c_void_p, C.c_int, C.c_int]
         _lib = L
     return _lib
 
@@ -397,3 +405,28 @@ def t2part(dist, o: T2partOptions):
     if rc != 0:
         raise RuntimeError(f"orc_t2part failed: {rc}")
     return {k: v.reshape((X, Y, Z), order="F") for k, v in outs.items()}
+
+
+# ---------------------------------------------------------------- synthetic input
+MOCK_DEFAULTS = dict(TE=10e-3, T1=1.0, FlipAngleRange=(140.0, 180.0), MyelinT2Range=(15e-3, 25e-3),
+                     MyelinFracRange=(0.05, 0.25), IET2Range=(60e-3, 90e-3), CSFT2Range=(1.0, 2.0),
+                     CSFFracRange=(0.0, 0.05), AmplitudeRange=(500.0, 2000.0), SNRRange=(50.0, 200.0),
+                     BackgroundFraction=0.0, BackgroundSigma=8.0)
+
+
+def mock_image(MatrixSize, nTE, seed=0, dtype=np.float64, nthreads=0, **kw):
+    """The benchmark's synthetic image (x, y, z, echo), byte for byte the
+    output of libdecaes_gpu's decaes_mock_image with the same options and seed,
+    made without loading the GPU library.  A leading z-slab of a volume equals
+    that volume's first slices."""
+    o = dict(MOCK_DEFAULTS, **kw)
+    co = _MockOpts(nTE, o["TE"], o["T1"], *[(C.c_double * 2)(*o[k]) for k in (
+        "FlipAngleRange", "MyelinT2Range", "MyelinFracRange", "IET2Range", "CSFT2Range", "CSFFracRange",
+        "AmplitudeRange", "SNRRange")], o["BackgroundFraction"], o["BackgroundSigma"])
+    X, Y, Z = (int(v) for v in MatrixSize)
+    img = np.empty((X, Y, Z, nTE), dtype=dtype, order="F")
+    rc = lib().orc_mock_image(C.byref(co), int(seed), X * Y * Z, img.ctypes.data_as(C.c_void_p),
+                              1 if img.dtype == np.float32 else 0, nthreads or (os.cpu_count() or 1))
+    if rc != 0:
+        raise ValueError("invalid mock image options")
+    return img
