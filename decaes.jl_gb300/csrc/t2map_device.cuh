@@ -1304,19 +1304,28 @@ static __device__ void process_voxel(Warp &w, long v) {
     }
     // fused T2partSEcorr window sums (src/T2partSEcorr.jl:95-138)
     if (P.fuse_t2part) {
-        double tsd = 0, ssp = 0, smp = 0, dsp = 0, dmp = 0, dw = 0;
+        // Each window sum runs in T2partSEcorr's loop order in a lane of its
+        // own (total, SPWin, MPWin, sigmoid weights), so the fused maps equal
+        // the standalone T2part of the saved distribution bit for bit.
+        const double *dv = w.s.w;
         bool anynan = false;
         #pragma unroll 1
-        for (int j = lane; j < n; j += 32) {
-            double d = w.s.w[j];
-            anynan |= isnan(d);
-            tsd = __dadd_rn(tsd, d);
-            if (j >= P.sp0 && j <= P.sp1) { dsp = __dadd_rn(dsp, __dmul_rn(d, P.logt2[j])); ssp = __dadd_rn(ssp, d); }
-            if (j >= P.mp0 && j <= P.mp1) { dmp = __dadd_rn(dmp, __dmul_rn(d, P.logt2[j])); smp = __dadd_rn(smp, d); }
-            if (P.weights) dw = __dadd_rn(dw, __dmul_rn(d, P.weights[j]));
-        }
+        for (int j = lane; j < n; j += 32) anynan |= isnan(dv[j]);
         anynan = __any_sync(FULL, anynan);
-        tsd = wsum(tsd); ssp = wsum(ssp); smp = wsum(smp); dsp = wsum(dsp); dmp = wsum(dmp); dw = wsum(dw);
+        double a0 = 0, a1 = 0;
+        if (lane == 0) {
+            #pragma unroll 1
+            for (int j = 0; j < n; ++j) a0 = __dadd_rn(a0, dv[j]);
+        } else if (lane == 1 || lane == 2) {
+            const int j0 = lane == 1 ? P.sp0 : P.mp0, j1 = lane == 1 ? P.sp1 : P.mp1;
+            #pragma unroll 1
+            for (int j = j0; j <= j1; ++j) { a0 = __dadd_rn(a0, __dmul_rn(dv[j], P.logt2[j])); a1 = __dadd_rn(a1, dv[j]); }
+        } else if (lane == 3 && P.weights) {
+            #pragma unroll 1
+            for (int j = 0; j < n; ++j) a0 = __dadd_rn(a0, __dmul_rn(dv[j], P.weights[j]));
+        }
+        const double tsd = __shfl_sync(FULL, a0, 0), dsp = __shfl_sync(FULL, a0, 1), ssp = __shfl_sync(FULL, a1, 1);
+        const double dmp = __shfl_sync(FULL, a0, 2), smp = __shfl_sync(FULL, a1, 2), dw = __shfl_sync(FULL, a0, 3);
         if (lane == 0 && !anynan) {
             if (tsd > 0) {
                 P.sfr[v] = P.weights ? dw / tsd : ssp / tsd;

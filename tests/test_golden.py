@@ -59,3 +59,26 @@ def test_gpu_reproduces_fixture(D, ctx, name):
     for k in ("alpha", "mu", "chi2factor", "gdn", "ggm", "resnorm"):
         np.testing.assert_allclose(maps[k], f["map_" + k], rtol=1e-8, atol=0, equal_nan=True, err_msg=k)
     print(f"{name}: dist bitwise {np.array_equal(dist, ref)}")
+
+
+@pytest.mark.gpu
+def test_mixed_method_on_the_tail_voxels(D, ctx):
+    """The mixed method on the benchmark volume's 13 voxels whose MWF moves by
+    more than 1e-3 against the FP64 method.  Their L-curves have several
+    curvature maxima within a few percent of each other, so the corner search
+    can settle on a neighbouring maximum when the Tikhonov solutions differ in
+    their last bits; the flip angle is unaffected.  Bound on these voxels:
+    |MWF| <= 0.03 and |alpha| <= 0.05 deg against the oracle (measured on the
+    full volume: 0.0215 and 0.0187 deg)."""
+    f = load("lcurve48_tail")
+    X, m, TE, n, T2, reg, K, extra = G.CASES["lcurve48_tail"]
+    o = D.T2mapOptions(MatrixSize=X, nTE=m, TE=TE, nT2=n, T2Range=T2, Reg=reg, nRefAngles=K, SaveRegParam=True,
+                       precision="mixed")
+    po = D.T2partOptions.from_t2map(o, SPWin=G.SPWIN, MPWin=G.MPWIN)
+    maps, dist, parts = D.T2mapSEcorr_T2partSEcorr(np.asfortranarray(f["image"]), o, po, ctx=ctx)
+    dm = np.abs(parts["sfr"] - f["part_sfr"]).ravel()
+    da = np.abs(maps["alpha"] - f["map_alpha"]).ravel()
+    dl = np.abs(np.log(maps["mu"]) - np.log(f["map_mu"])).ravel()
+    print("MWF", np.round(dm, 5), "alpha", np.round(da, 5), "|dlog mu|", np.round(dl, 3))
+    assert dm.max() <= 0.03
+    assert da.max() <= 0.05

@@ -65,12 +65,15 @@ def test_t2map_matches_oracle(D, orc, ctx, name):
 
 
 def test_plain_method_is_bitwise(D, orc, ctx):
-    """The FP64 path and the oracle agree bit for bit (dist, alpha, mu)."""
+    """The FP64 path and the oracle agree bit for bit (dist, alpha, mu, and
+    the fused T2part maps)."""
     c = CASES["lcurve"]
     img, o, maps, dist, parts, om, od, op = run_case(D, orc, ctx, c, seed=5)
     np.testing.assert_array_equal(dist, od)
     np.testing.assert_array_equal(maps["alpha"], om["alpha"])
     np.testing.assert_array_equal(maps["mu"], om["mu"])
+    for k in ("sfr", "sgm", "mfr", "mgm"):
+        np.testing.assert_array_equal(parts[k], op[k], err_msg=k)
 
 
 def test_float32_input(D, orc, ctx):
