@@ -545,10 +545,12 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed", "mixed_tc"],
                     help="method of the headline value; with mixed the FP64 method is measured beside it")
     ap.add_argument("--no-fp64-compare", action="store_true",
                     help="skip the FP64 comparison run of the mixed headline")
+    ap.add_argument("--no-tc-compare", action="store_true",
+                    help="skip the run of the mixed method with tensor-core grid products beside the mixed headline")
     ap.add_argument("--workload", default="lcurve48", choices=sorted(WORKLOADS) + ["batch", "serve"],
                     help="lcurve48 (headline), gcv56, chi2k8_48, batch (uneven volumes in one launch), serve")
     ap.add_argument("--nvol", type=int, default=256, help="volumes of --workload batch")
@@ -622,6 +624,19 @@ def main():
     d2h = sum(v.numel() * 4 for v in h_out.values()) + sum(v.numel() * 4 for v in h_parts.values())
     del h_out, h_parts, h_img
 
+    # ---- the mixed method with the search's grid products on the tensor cores ----
+    tc = None
+    if args.precision == "mixed" and not args.no_tc_compare:
+        motc, potc, _ = workload(matrix, "mixed_tc", args.workload)
+        runtc = DeviceRun(D, _lib, ctx, torch, motc, potc, img, V)
+        ktc = max(1, min(args.steps, 3))
+        ms_tc, launches_tc, solve_tc = runtc.timed(ktc, 1, world)
+        st_tc = runtc.stats()
+        tc = {"ms_per_step": ms_tc, "steps": ktc, "value": replicas.aggregate_voxels_per_s(V, ms_tc, world),
+              "grid_products_ms": st_tc["ms_grid_products"], "grid_product_launches": st_tc["grid_product_launches"],
+              "grid_product_failures": st_tc["grid_product_failures"], "host": runtc.host()}
+        del runtc
+
     # ---- the FP64 method on the volume (or its leading slices), FP64 outputs ----
     flat = img.reshape((V, -1), order="F")
     nz = matrix[2]
@@ -674,6 +689,27 @@ def main():
         e = line["mixed_vs_fp64"]["errors"]
         line["mixed_vs_fp64"]["gate_met"] = bool(e["mwf_abs"]["p99"] <= 1e-3 and e["same_processed_voxels"])
 
+    if tc is not None:
+        # the grid-product GEMM's work: 2 x 6 slice-pair products x K*nT2 x nTE per voxel
+        w_ = WORKLOADS[args.workload]
+        gemm_flops = 2.0 * 6 * w_["K"] * w_["nT2"] * (-(-w_["nTE"] // 16) * 16) * Vp
+        gemm_bytes = (w_["K"] * w_["nT2"] * 4.0 + 4.0 + 4.0 * w_["nTE"]) * Vp
+        line["tensor_core_grid_products"] = {
+            "method": "mixed_tc: the search's A_k'b for every grid angle from one tcgen05 GEMM per 2^19 voxels "
+                      "(3 bf16 fixed-point slices per operand, exact FP32 accumulation), read by the voxel kernel",
+            "value": tc["value"], "ms_per_step": tc["ms_per_step"], "steps": tc["steps"],
+            "speedup_vs_mixed": ms_per_step / tc["ms_per_step"],
+            "gemm_ms_per_step": tc["grid_products_ms"], "gemm_launches": tc["grid_product_launches"],
+            "gemm_failures": tc["grid_product_failures"],
+            "gemm_tflops": gemm_flops / (tc["grid_products_ms"] * 1e-3) / 1e12 if tc["grid_products_ms"] else None,
+            "gemm_gbs": gemm_bytes / (tc["grid_products_ms"] * 1e-3) / 1e9 if tc["grid_products_ms"] else None,
+            "gemm_work": "2 x 6 slice-pair products x K*nT2 x nTE(padded to 16) per above-threshold voxel; "
+                         "bytes = K*nT2 FP32 products + exponent + the FP32 echo train per voxel",
+        }
+        if fp64 is not None:
+            line["tensor_core_grid_products"]["errors_vs_fp64"] = method_errors(
+                *(a[:Vs] for a in tc["host"]), *fp64)
+
     # ---- the oracle on a sample: CPU baseline and parity at this scale ----
     peak = fp64_peak_tflops(torch)
     kern_ms = statistics.median(solve_ms)
@@ -699,11 +735,16 @@ def main():
                 "gate": "per-bin relative <= 1e-8 and |MWF| <= 1e-10",
                 "gate_met": bool(e64["dist_bin_rel"]["max"] <= 1e-8 and e64["mwf_abs"]["max"] <= 1e-10
                                  and e64["same_processed_voxels"])}
-        if args.precision == "mixed":
+        if args.precision in ("mixed", "mixed_tc"):
             dm, am, sm = (x[pk] for x in head)
             em = method_errors(dm, am, sm, o_d, o_a, o_s)
             par["mixed_vs_oracle"] = {**em, "gate": "MWF |mixed - oracle| p99 <= 1e-3",
                                       "gate_met": bool(em["mwf_abs"]["p99"] <= 1e-3 and em["same_processed_voxels"])}
+        if tc is not None:
+            dm, am, sm = (x[pk] for x in tc["host"])
+            em = method_errors(dm, am, sm, o_d, o_a, o_s)
+            par["mixed_tc_vs_oracle"] = {**em, "gate": "MWF |mixed_tc - oracle| p99 <= 1e-3",
+                                         "gate_met": bool(em["mwf_abs"]["p99"] <= 1e-3 and em["same_processed_voxels"])}
         line["parity"] = par
     if args.precision == "fp64":
         if cb is not None:

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "decaes_gpu.h"
+#include "decaes_tc.h"
 #include "epg.cuh"
 #include "host.h"
 #include "voxel_kernels.cuh"
@@ -240,6 +241,7 @@ struct Basis {
     double *t2 = nullptr, *logt2 = nullptr, *angles = nullptr, *As = nullptr, *dAs = nullptr, *fixed = nullptr;
     double *Gs = nullptr;   // packed Gram matrices of the grid (or fixed) bases, made on first use by the mixed method
     double *AsT = nullptr;  // the same bases transposed (mixed method)
+    unsigned char *Bsl = nullptr;  // the grid bases as bf16 slices for the tensor-core products (DECAES_PREC_MIXED_TC)
     std::vector<double> h_t2, h_angles;
     size_t bytes = 0;
     long last_use = 0;
@@ -261,6 +263,11 @@ struct Tune {
 
 }  // namespace
 
+// Voxel-list positions per tensor-core product launch (its F buffer holds
+// this many rows of K*nT2 floats), and the launches whose time is recorded.
+constexpr long kTcChunk = 1L << 19;
+constexpr int kTcEvents = 16;
+
 struct decaes_ctx {
     int device = 0;
     size_t budget = 0, used = 0;
@@ -275,6 +282,8 @@ struct decaes_ctx {
     size_t smem_optin = 0;
     std::map<TuneKey, Tune> tune;
     int force_wpb = 0;  // autotuner trials
+    int tc_chunks = 0;                 // tensor-core product launches of the last call
+    cudaEvent_t tc_ev[2 * kTcEvents];  // their start/end events (the first kTcEvents)
     std::mutex mu;
 };
 
@@ -309,6 +318,9 @@ int buf(decaes_ctx *ctx, const std::string &name, size_t bytes, void **out) {
 
 size_t esize(int dtype) { return dtype == DECAES_F32 ? 4 : 8; }
 
+// The mixed method, with the grid products from the CUDA cores or the tensor cores.
+bool is_mixed(const decaes_t2map_opts &o) { return o.precision == DECAES_PREC_MIXED || o.precision == DECAES_PREC_MIXED_TC; }
+
 // Resident per-parameter basis: T2 grid, angle grid, As and dAs (or the fixed basis).
 int get_basis(decaes_ctx *ctx, const decaes_t2map_opts &o, Basis **out) {
     const bool fixed = !std::isnan(o.SetFlipAngle);
@@ -329,7 +341,7 @@ int get_basis(decaes_ctx *ctx, const decaes_t2map_opts &o, Basis **out) {
     if (lru != ctx->bases.end()) {
         Basis &b = lru->second;
         cudaFree(b.t2); cudaFree(b.logt2); cudaFree(b.angles); cudaFree(b.As); cudaFree(b.dAs); cudaFree(b.fixed);
-        cudaFree(b.Gs); cudaFree(b.AsT);
+        cudaFree(b.Gs); cudaFree(b.AsT); cudaFree(b.Bsl);
         ctx->used -= b.bytes;
         ctx->bases.erase(lru);
     }
@@ -389,7 +401,7 @@ int prepare_basis(decaes_ctx *ctx, const decaes_t2map_opts &o, cudaStream_t st, 
     if (n > 256) return fail(ctx, DECAES_EINVAL, "nT2 > 256 is not supported by libdecaes_gpu");
     const bool fixed = !std::isnan(o.SetFlipAngle);
     if (!fixed && o.nRefAngles > 256) return fail(ctx, DECAES_EINVAL, "nRefAngles > 256 is not supported by libdecaes_gpu");
-    const bool mixed = o.precision == DECAES_PREC_MIXED;
+    const bool mixed = is_mixed(o);
     if (mixed && n > dk::kGramMaxN)
         return fail(ctx, DECAES_EINVAL, "precision = mixed supports nT2 <= " + std::to_string(dk::kGramMaxN));
     Basis *B;
@@ -407,6 +419,17 @@ int prepare_basis(decaes_ctx *ctx, const decaes_t2map_opts &o, cudaStream_t st, 
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(ctx->stream));
     }
+    if (o.precision == DECAES_PREC_MIXED_TC && !fixed && !B->Bsl) {
+        const int K = o.nRefAngles;
+        const size_t sb = (size_t)dk::tc_ntiles(K, n) * dk::kTcSlices * dk::tc_slice_bytes(dk::kTcTileN, dk::tc_mpad(m));
+        if (ctx->used + sb > ctx->budget) return fail(ctx, DECAES_ENOMEM, "grid-basis slices exceed the HBM budget");
+        CK(cudaMalloc(&B->Bsl, sb));
+        B->bytes += sb;
+        ctx->used += sb;
+        CK(dk::tc_make_basis_slices(B->As, m, n, K, B->Bsl, ctx->stream));
+        ++*launches;
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
     *out = B;
     return DECAES_OK;
 }
@@ -418,7 +441,7 @@ int make_params(decaes_ctx *ctx, const decaes_t2map_opts &o, const dh::T2partPla
                 long *wsm) {
     const int m = o.nTE, n = o.nT2;
     const long V = (long)o.MatrixSize[0] * o.MatrixSize[1] * o.MatrixSize[2];
-    const bool fixed = !std::isnan(o.SetFlipAngle), mixed = o.precision == DECAES_PREC_MIXED;
+    const bool fixed = !std::isnan(o.SetFlipAngle), mixed = is_mixed(o);
     P = dk::Params{};
     P.m = m; P.n = n; P.K = fixed ? 1 : o.nRefAngles; P.M = m + n; P.lda = (m + n) | 1;
     P.reg = o.Reg; P.chi2factor = o.Chi2Factor; P.noiselevel = o.NoiseLevel;
@@ -460,7 +483,7 @@ int make_params(decaes_ctx *ctx, const decaes_t2map_opts &o, const dh::T2partPla
 int tuned_wpb_or0(decaes_ctx *ctx, const decaes_t2map_opts &o) {
     if (ctx->force_wpb) return ctx->force_wpb;
     const bool fixed = !std::isnan(o.SetFlipAngle);
-    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, o.precision == DECAES_PREC_MIXED, o.RefConAngle == 180.0,
+    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, is_mixed(o), o.RefConAngle == 180.0,
               o.legacy != 0};
     auto it = ctx->tune.find(k);
     return it == ctx->tune.end() ? 0 : it->second.wpb;
@@ -553,7 +576,7 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
     P.smem_stride = wsm;
     int wpb = tuned_wpb(ctx, o), grid = 0;
     size_t smem = 0;
-    auto kern = o.legacy ? dk::k_voxels_legacy : (o.precision == DECAES_PREC_MIXED ? dk::k_voxels_mixed : dk::k_voxels_plain);
+    auto kern = o.legacy ? dk::k_voxels_legacy : (is_mixed(o) ? dk::k_voxels_mixed : dk::k_voxels_plain);
     // the plain method's large workspace: blocks of up to 8 warps can hold a
     // warp per SM more than single-warp blocks (its kernel allows 256 threads)
     if (kern == dk::k_voxels_plain && tuned_wpb_or0(ctx, o) == 0) wpb = most_warps_wpb(ctx, kern, wsm, 8);
@@ -561,10 +584,44 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
     void *scr;
     if (int rc = buf(ctx, "scratch", sizeof(double) * (size_t)P.scr_stride * grid * wpb, &scr)) return rc;
     P.scratch = (double *)scr;
-    cudaEventRecord(ctx->ev[2], st);
-    kern<<<grid, 32 * wpb, smem, st>>>(P);
-    cudaEventRecord(ctx->ev[3], st);
-    ++nl;
+    ctx->tc_chunks = 0;
+    if (o.precision == DECAES_PREC_MIXED_TC && P.angle_mode == 0) {
+        // The search's grid products on the tensor cores, a chunk of the voxel
+        // list at a time (bounded F buffer): products of the chunk, then the
+        // chunk's voxel solve.  The host does not know the list's length, so
+        // chunks past it launch and return at once.
+        const int mpad = dk::tc_mpad(o.nTE), ntiles = dk::tc_ntiles(o.nRefAngles, n);
+        const long ldF = (long)ntiles * dk::kTcTileN;
+        const long C = std::max<long>(dk::kTcTileM, std::min<long>(kTcChunk, V));
+        void *F, *Fexp;
+        if (int rc = buf(ctx, "tc_products", sizeof(float) * (size_t)C * ldF, &F)) return rc;
+        if (int rc = buf(ctx, "tc_exponents", sizeof(int) * (size_t)C, &Fexp)) return rc;
+        dk::TcParams T{};
+        T.image = d_image; T.f32 = dtype == DECAES_F32; T.V = V; T.m = o.nTE; T.mpad = mpad;
+        T.vidx = (const int *)vidx; T.nvox = d_nvox; T.Bsl = B->Bsl; T.ntiles = ntiles;
+        T.F = (float *)F; T.ldF = ldF; T.Fexp = (int *)Fexp; T.err = (unsigned *)((char *)cnt + 32);
+        P.Fk = (const float *)F; P.Fexp = (const int *)Fexp; P.ldF = ldF;
+        cudaEventRecord(ctx->ev[2], st);
+        for (long c0 = 0; c0 < V; c0 += C) {
+            const int q = ctx->tc_chunks < kTcEvents ? ctx->tc_chunks : -1;
+            T.t0 = c0; T.t1 = c0 + C;
+            if (q >= 0) cudaEventRecord(ctx->tc_ev[2 * q], st);
+            CK(dk::tc_grid_products(T, ctx->sms, st));
+            if (q >= 0) cudaEventRecord(ctx->tc_ev[2 * q + 1], st);
+            if (c0 > 0) CK(cudaMemsetAsync(d_counter, 0, sizeof(int), st));
+            P.tq0 = c0; P.tq1 = c0 + C;
+            kern<<<grid, 32 * wpb, smem, st>>>(P);
+            nl += 2;
+            ctx->tc_chunks++;
+            CK(cudaGetLastError());
+        }
+        cudaEventRecord(ctx->ev[3], st);
+    } else {
+        cudaEventRecord(ctx->ev[2], st);
+        kern<<<grid, 32 * wpb, smem, st>>>(P);
+        cudaEventRecord(ctx->ev[3], st);
+        ++nl;
+    }
     CK(cudaGetLastError());
     *launches += nl;
     return DECAES_OK;
@@ -683,6 +740,7 @@ extern "C" decaes_ctx *decaes_create(int device, size_t hbm_budget_bytes) {
     c->smem_optin = prop.sharedMemPerBlockOptin;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return nullptr; }
     for (auto &e : c->ev) cudaEventCreate(&e);
+    for (auto &e : c->tc_ev) cudaEventCreate(&e);
     return c;
 }
 
@@ -694,9 +752,10 @@ extern "C" void decaes_destroy(decaes_ctx *ctx) {
     for (auto &kv : ctx->bases) {
         Basis &b = kv.second;
         cudaFree(b.t2); cudaFree(b.logt2); cudaFree(b.angles); cudaFree(b.As); cudaFree(b.dAs); cudaFree(b.fixed);
-        cudaFree(b.Gs); cudaFree(b.AsT);
+        cudaFree(b.Gs); cudaFree(b.AsT); cudaFree(b.Bsl);
     }
     for (auto &e : ctx->ev) cudaEventDestroy(e);
+    for (auto &e : ctx->tc_ev) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -855,14 +914,24 @@ extern "C" int decaes_sync_stats(decaes_ctx *ctx, void *stream) {
     if (int rc = buf(ctx, "counters", 64, &cnt)) return rc;
     int hn;
     unsigned long long hs[2];
+    unsigned herr = 0;
     CK(cudaMemcpy(&hn, cnt, sizeof(int), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(hs, (char *)cnt + 16, sizeof hs, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&herr, (char *)cnt + 32, sizeof herr, cudaMemcpyDeviceToHost));
     float t;
     ctx->stats.voxels_processed = hn;
     ctx->stats.nnls_cap_hits = (int64_t)hs[0];
     ctx->stats.search_limit_hits = (int64_t)hs[1];
     cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[5]); ctx->stats.ms_total = t;
     cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]); ctx->stats.ms_solve = t;
+    double gp = 0.0;
+    for (int q = 0; q < std::min(ctx->tc_chunks, kTcEvents); ++q) {
+        cudaEventElapsedTime(&t, ctx->tc_ev[2 * q], ctx->tc_ev[2 * q + 1]);
+        gp += t;
+    }
+    ctx->stats.ms_grid_products = gp;
+    ctx->stats.grid_product_launches = ctx->tc_chunks;
+    ctx->stats.grid_product_failures = herr;
     return DECAES_OK;
 }
 
@@ -974,7 +1043,7 @@ struct BatchPrep {
 // Relative cost of a voxel: the autotuner's measurement, else a model of the
 // methods' measured costs (FP64 GCV ~35x the mixed method, FP64 ~5x mixed).
 double voxel_cost(decaes_ctx *ctx, const decaes_t2map_opts &o) {
-    const bool fixed = !std::isnan(o.SetFlipAngle), mixed = o.precision == DECAES_PREC_MIXED;
+    const bool fixed = !std::isnan(o.SetFlipAngle), mixed = is_mixed(o);
     TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, mixed, o.RefConAngle == 180.0, o.legacy != 0};
     auto it = ctx->tune.find(k);
     if (it != ctx->tune.end() && it->second.us_per_voxel > 0) return it->second.us_per_voxel;
@@ -1062,7 +1131,7 @@ int batch_plan(decaes_ctx *ctx, const decaes_volume *vols, int nvol, cudaStream_
         for (int q = c.first; q < c.first + c.count; ++q) {
             const decaes_t2map_opts &o = bp.vols[q].v.mopts;
             legacy = legacy || o.legacy;
-            (o.precision == DECAES_PREC_MIXED ? any_mixed : any_plain) = true;
+            (is_mixed(o) ? any_mixed : any_plain) = true;
         }
         c.kern = dk::batch_kernel(legacy, any_plain, any_mixed);
         c.wpb = tuned_wpb(ctx, bp.vols[c.first].v.mopts);
@@ -1337,7 +1406,7 @@ extern "C" int decaes_autotune(decaes_ctx *ctx, const decaes_t2map_opts *opts, d
     }
     ctx->force_wpb = 0;
     const bool fixed = !std::isnan(o.SetFlipAngle);
-    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, o.precision == DECAES_PREC_MIXED, o.RefConAngle == 180.0,
+    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, is_mixed(o), o.RefConAngle == 180.0,
               o.legacy != 0};
     Tune t;
     t.wpb = best_w;
@@ -1628,7 +1697,7 @@ std::vector<Chunk> srv_launch_tick(decaes_server *S) {
         bool legacy = false, any_plain = false, any_mixed = false;
         for (int q = k.first; q < k.first + k.count; ++q) {
             legacy = legacy || ch[q].r->mo.legacy;
-            (ch[q].r->mo.precision == DECAES_PREC_MIXED ? any_mixed : any_plain) = true;
+            (is_mixed(ch[q].r->mo) ? any_mixed : any_plain) = true;
         }
         k.kern = dk::batch_kernel(legacy, any_plain, any_mixed);
         k.wpb = tuned_wpb(ctx, ch[k.first].r->mo);

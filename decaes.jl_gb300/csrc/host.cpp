@@ -218,7 +218,8 @@ std::string check_t2map(const decaes_t2map_opts &o) {
         return "Refocusing control angle must be in the range [0, 180], but RefConAngle = " + jlfmt(o.RefConAngle) + ".";
     if (!std::isnan(o.SetFlipAngle) && !(0.0 <= o.SetFlipAngle && o.SetFlipAngle <= 180.0))
         return "Fixed flip angle must be in the range [0, 180], but SetFlipAngle = " + jlfmt(o.SetFlipAngle) + ".";
-    if (o.precision != DECAES_PREC_FP64 && o.precision != DECAES_PREC_MIXED) return "precision must be DECAES_PREC_FP64 or DECAES_PREC_MIXED.";
+    if (o.precision != DECAES_PREC_FP64 && o.precision != DECAES_PREC_MIXED && o.precision != DECAES_PREC_MIXED_TC)
+        return "precision must be DECAES_PREC_FP64, DECAES_PREC_MIXED or DECAES_PREC_MIXED_TC.";
     return "";
 }
 

@@ -131,6 +131,17 @@ static __device__ __noinline__ void gram_rhs_t(GramWS &g, const double *AT, int 
     __syncwarp();
 }
 
+// f = A'b from a precomputed row of products in FP32 (the tensor-core grid
+// products of the voxel), times their scale to the normalized decay.
+static __device__ __noinline__ void gram_rhs_f32(GramWS &g, const float *F, int n, double scale, int m,
+                                                 const double *b) {
+    const int lane = threadIdx.x & 31;
+    #pragma unroll 1
+    for (int j = lane; j < n; j += 32) g.f[j] = widen(__ldg(F + j)) * scale;
+    gram_bb(g, m, b);
+    __syncwarp();
+}
+
 // f = A'b and G = A'A from a basis staged in shared memory as FP32 values
 // (column-major, odd leading dimension lda).  The staged values are the FP32
 // EPG curves themselves, so the products are exact in FP64 and G is the Gram

@@ -3,6 +3,7 @@
 // save_results!/T2part epilogue (src/T2mapSEcorr.jl:201-238, 409-591;
 // src/lsqnonneg.jl; src/splines.jl; src/optimization.jl; src/T2partSEcorr.jl).
 #pragma once
+#include <climits>
 #include "epg.cuh"
 #include "nnls_gram.cuh"
 #include "legacy.cuh"
@@ -54,6 +55,9 @@ struct Warp {
     float *As32;   // FP32 basis staged in shared memory, column-major, leading dimension ldA
     int ldA;
     bool mixed;    // the mixed method (Params::mixed)
+    long slot;     // the voxel's position in this launch's part of the voxel list
+    bool fk_ok;    // its tensor-core grid products are usable
+    double fscale; // and their scale to the normalized decay: 2^e / max
 };
 // The warp's method, folded to a constant in single-method kernels.
 __device__ __forceinline__ bool use_mixed(const Warp &w) { return kHasMixed && (!kHasPlain || w.mixed); }
@@ -902,7 +906,10 @@ static __device__ void fa_update(Search &S, int I) {
     if (use_mixed(w)) {
         // precomputed Gram matrix of grid basis I; A'b from its transposed copy
         gram_load(w.g, P.Gs + (long)(I - 1) * (n * (n + 1) / 2), n);
-        gram_rhs_t(w.g, P.AsT + (long)(I - 1) * m * n, m, n, w.data);
+        if (w.fk_ok)  // from the tensor-core grid products
+            gram_rhs_f32(w.g, P.Fk + w.slot * P.ldF + (long)(I - 1) * n, n, w.fscale, m, w.data);
+        else
+            gram_rhs_t(w.g, P.AsT + (long)(I - 1) * m * n, m, n, w.data);
         r = gram_nnls(w.g, w.s.x, w.s.w, w.s.idx, n, 0.0, 3 * n, &w.g.lastk);
     } else {
         r = warp_lsq(w.s, A, m, n, w.data, false, 0.0);
@@ -1191,6 +1198,12 @@ static __device__ void process_voxel(Warp &w, long v) {
         #pragma unroll 1
         for (int i = lane; i < m; i += 32) w.data[i] = w.data[i] / mx;
     __syncwarp();
+    w.fk_ok = false;
+    if (use_mixed(w) && P.Fk) {
+        const int e = P.Fexp[w.slot];
+        w.fk_ok = e != INT_MIN;
+        w.fscale = w.fk_ok ? ldexp(1.0, e) / (mx > 0 ? mx : 1.0) : 0.0;
+    }
 
     double alpha;
     w.g.lastk = 0;  // warm starts never cross voxels (results independent of scheduling)

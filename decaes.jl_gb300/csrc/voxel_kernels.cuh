@@ -76,12 +76,14 @@ __device__ __forceinline__ void voxels_body(const Params &P) {
     w.nnls_caps = 0;
     w.loop_caps = 0;
     warp_setup(w, P, smem + (long)wib * P.smem_stride, P.scratch + ((long)blockIdx.x * wpb + wib) * P.scr_stride);
-    const int nvox = *P.nvox;
+    const long nvox = P.tq1 > 0 && P.tq1 < (long)*P.nvox ? P.tq1 : (long)*P.nvox;
     for (;;) {
-        int t = 0;
-        if (w.lane == 0) t = atomicAdd(P.counter, 1);
-        t = __shfl_sync(FULL, t, 0);
+        int q = 0;
+        if (w.lane == 0) q = atomicAdd(P.counter, 1);
+        q = __shfl_sync(FULL, q, 0);
+        const long t = P.tq0 + q;
         if (t >= nvox) break;
+        w.slot = q;
         process_voxel(w, (long)P.vidx[t]);
     }
     if (w.lane == 0) {
@@ -133,6 +135,7 @@ __device__ __forceinline__ void voxels_batch_body(const BatchParams &B) {
             warp_setup(w, *Pw, ws, scr);
             cur = lo;
         }
+        w.slot = t - B.offsets[lo];
         process_voxel(w, (long)Pw->vidx[t - B.offsets[lo]]);
     }
     if (cur >= 0 && w.lane == 0) {

@@ -12,7 +12,7 @@ from . import build as _build
 
 F32, F64 = 0, 1
 REG = {"none": 0, "lcurve": 1, "gcv": 2, "chi2": 3, "mdp": 4}
-PREC = {"fp64": 0, "mixed": 1}
+PREC = {"fp64": 0, "mixed": 1, "mixed_tc": 2}
 ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENOMEM", 4: "ELEGACY"}
 
 _vp = C.c_void_p
@@ -47,7 +47,8 @@ class StatsC(C.Structure):
     _fields_ = [("voxels", C.c_int64), ("voxels_processed", C.c_int64), ("nnls_cap_hits", C.c_int64),
                 ("search_limit_hits", C.c_int64), ("ms_total", C.c_double), ("ms_solve", C.c_double),
                 ("ms_h2d", C.c_double), ("ms_d2h", C.c_double), ("solve_launches", C.c_int32),
-                ("kernel_launches", C.c_int32)]
+                ("kernel_launches", C.c_int32), ("ms_grid_products", C.c_double),
+                ("grid_product_launches", C.c_int32), ("grid_product_failures", C.c_int32)]
 
 
 class MockOptsC(C.Structure):

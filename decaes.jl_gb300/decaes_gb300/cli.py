@@ -83,8 +83,9 @@ def build_parser() -> argparse.ArgumentParser:
     g.add_argument("--betargs", type=str, default="-m -n -f 0.25 -R", help="BET arguments, space or comma separated")
     g.add_argument("--betpath", type=str, default="bet", help="path of the BET executable")
     g = p.add_argument_group("GPU")
-    g.add_argument("--precision", choices=("fp64", "mixed"), default="fp64",
-                   help="fp64: the reference's arithmetic; mixed: the mixed-precision method")
+    g.add_argument("--precision", choices=("fp64", "mixed", "mixed_tc"), default="fp64",
+                   help="fp64: the reference's arithmetic; mixed: the mixed-precision method; mixed_tc: the mixed "
+                        "method with the flip-angle search's grid products on the tensor cores")
     g.add_argument("--device", type=int, default=0, help="CUDA device")
     return p
 

@@ -47,7 +47,8 @@ end
 CT2mapOpts(o::T2mapOptions; precision::Symbol = :fp64) = CT2mapOpts(
     Int32.(o.MatrixSize), o.nTE, o.TE, o.nT2, Float64.(o.T2Range), o.T1, o.Threshold, o.MinRefAngle, o.nRefAngles,
     o.nRefAnglesMin, REG[o.Reg], nan_or(o.Chi2Factor), nan_or(o.NoiseLevel), o.RefConAngle, nan_or(o.SetFlipAngle),
-    o.SaveResidualNorm, o.SaveDecayCurve, o.SaveRegParam, o.SaveNNLSBasis, o.legacy, precision === :mixed ? 1 : 0)
+    o.SaveResidualNorm, o.SaveDecayCurve, o.SaveRegParam, o.SaveNNLSBasis, o.legacy,
+    precision === :mixed ? 1 : precision === :mixed_tc ? 2 : 0)
 
 # decaes_t2map_out (16 pointers)
 struct CT2mapOut

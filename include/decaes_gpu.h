@@ -37,8 +37,13 @@ enum { DECAES_REG_NONE = 0, DECAES_REG_LCURVE = 1, DECAES_REG_GCV = 2, DECAES_RE
  * work on the normal equations (FP64 Gram matrix, LDL' updates, warm-started
  * active sets); root finding, curvature, the spline fit and every solve stay
  * FP64.  MIXED results differ from FP64 by |MWF| <= 1e-3 (measured p99 ~1e-5);
- * it needs nT2 <= 64. */
-enum { DECAES_PREC_FP64 = 0, DECAES_PREC_MIXED = 1 };
+ * it needs nT2 <= 64.  MIXED_TC is MIXED with the flip-angle search's grid
+ * products A_k'b (every grid angle, every voxel) computed beforehand as one
+ * tensor-core GEMM per chunk of voxels (bf16 fixed-point slices, exact FP32
+ * accumulation, ~2^-24 relative error); it applies to the single-volume entry
+ * points when the flip angle is searched, and batches and the server run
+ * MIXED_TC volumes as MIXED.  No counterpart in the reference (an extension). */
+enum { DECAES_PREC_FP64 = 0, DECAES_PREC_MIXED = 1, DECAES_PREC_MIXED_TC = 2 };
 enum {
     DECAES_OK = 0,
     DECAES_EINVAL = 1,   /* invalid option or argument (reference AssertionError) */
@@ -116,6 +121,10 @@ typedef struct {
     double ms_h2d, ms_d2h;     /* device time of the host<->device copies */
     int32_t solve_launches;    /* voxel-solve kernel launches of the call */
     int32_t kernel_launches;   /* all kernels launched by the call */
+    double ms_grid_products;   /* DECAES_PREC_MIXED_TC: device time of the tensor-core grid products */
+    int32_t grid_product_launches;
+    int32_t grid_product_failures; /* their thread blocks that gave up a bounded wait (the voxels
+                                      concerned then form their products on the CUDA cores) */
 } decaes_stats;
 
 /* ---- context -------------------------------------------------------------

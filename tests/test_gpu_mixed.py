@@ -1,4 +1,6 @@
-"""The mixed-precision method (DECAES_PREC_MIXED) against the FP64 oracle.
+"""The mixed-precision method (DECAES_PREC_MIXED, and DECAES_PREC_MIXED_TC with
+the flip-angle search's grid products on the tensor cores) against the FP64
+oracle.
 
 The mixed method solves the same problems with a different algorithm
 (normal-equation Lawson-Hanson with warm starts, FP32 EPG at the fitted angle),
@@ -32,14 +34,14 @@ CASES = {
 }
 
 
-def mixed_vs_oracle(D, orc, ctx, c, seed=21):
+def mixed_vs_oracle(D, orc, ctx, c, seed=21, precision="mixed"):
     img = D.mock_image(D.MockImageOptions(MatrixSize=c["X"], nTE=c["m"], TE=c["TE"],
                                           BackgroundFraction=c.get("bg", 0.0)), seed=seed)
     kw = dict(MatrixSize=c["X"], nTE=c["m"], TE=c["TE"], nT2=c["n"], T2Range=c["T2"], Reg=c["Reg"],
               nRefAngles=c["K"], Chi2Factor=c.get("Chi2Factor"), NoiseLevel=c.get("NoiseLevel"),
               Threshold=c.get("thr", 0.0), RefConAngle=c.get("RefConAngle", 180.0),
               SetFlipAngle=c.get("SetFlipAngle"), SaveRegParam=True, SaveResidualNorm=True)
-    o = D.T2mapOptions(**kw, precision="mixed")
+    o = D.T2mapOptions(**kw, precision=precision)
     po = D.T2partOptions.from_t2map(o, SPWin=SPWIN, MPWin=MPWIN)
     maps, dist, parts = D.T2mapSEcorr_T2partSEcorr(img, o, po, ctx=ctx)
     om, od = orc.t2map(img, orc_opts(orc, D.T2mapOptions(**kw)), nthreads=8)
@@ -60,15 +62,21 @@ def errors(c, maps, dist, parts, om, od, op):
                 l1_p99=float(np.quantile(l1, 0.99)), l1_max=float(l1.max()), alpha_max=float(da.max()))
 
 
+@pytest.mark.parametrize("precision", ["mixed", "mixed_tc"])
 @pytest.mark.parametrize("name", list(CASES))
-def test_mixed_within_gate(D, orc, ctx, name):
+def test_mixed_within_gate(D, orc, ctx, name, precision):
     c = CASES[name]
-    maps, dist, parts, om, od, op = mixed_vs_oracle(D, orc, ctx, c)
+    maps, dist, parts, om, od, op = mixed_vs_oracle(D, orc, ctx, c, precision=precision)
+    if precision == "mixed_tc":
+        st = ctx.stats()
+        searched = c.get("SetFlipAngle") is None
+        assert st["grid_product_launches"] == (1 if searched else 0)
+        assert st["grid_product_failures"] == 0
     # same voxels processed, same NaN pattern
     np.testing.assert_array_equal(np.isnan(dist), np.isnan(od))
     np.testing.assert_array_equal(np.isnan(parts["sfr"]), np.isnan(op["sfr"]))
     e = errors(c, maps, dist, parts, om, od, op)
-    print(f"{name}: {e}")
+    print(f"{name} {precision}: {e}")
     assert e["mwf_max"] <= MWF_GATE
     assert e["l1_p99"] <= DIST_L1_P99
     assert e["alpha_max"] <= ALPHA_ATOL
@@ -85,3 +93,25 @@ def test_mixed_deterministic(D, ctx):
     m2, d2 = D.T2mapSEcorr(img, o, ctx=ctx)
     np.testing.assert_array_equal(d1, d2)
     np.testing.assert_array_equal(m1["alpha"], m2["alpha"])
+
+
+def test_tensor_core_products_across_chunks(D, ctx):
+    """The tensor-core grid products run a chunk of 2^19 voxel-list positions
+    at a time; voxels from all over the list (both chunks) give the same
+    results as in a run of their own (each voxel's products and solve depend
+    only on its own echo train)."""
+    X = (1024, 513, 1)  # 525,312 voxels: one full chunk and the start of the next
+    m = 32
+    img = D.mock_image(D.MockImageOptions(MatrixSize=X, nTE=m, TE=10e-3), seed=8, dtype=np.float32)
+    kw = dict(nTE=m, TE=10e-3, nT2=40, T2Range=(10e-3, 2.0), Reg="chi2", Chi2Factor=1.02, nRefAngles=8,
+              precision="mixed_tc")
+    o = D.T2mapOptions(MatrixSize=X, **kw)
+    maps, dist = D.T2mapSEcorr(img, o, ctx=ctx)
+    st = ctx.stats()
+    assert st["grid_product_launches"] == 2 and st["grid_product_failures"] == 0
+    flat = img.reshape((-1, m), order="F")
+    pick = np.arange(0, flat.shape[0], 997)  # spread over the list, so both chunks are sampled
+    sub = flat[pick].reshape((len(pick), 1, 1, m), order="F")
+    m1, d1 = D.T2mapSEcorr(sub, D.T2mapOptions(MatrixSize=(len(pick), 1, 1), **kw), ctx=ctx)
+    np.testing.assert_array_equal(dist.reshape(-1, 40, order="F")[pick], d1.reshape(-1, 40, order="F"))
+    np.testing.assert_array_equal(maps["alpha"].reshape(-1, order="F")[pick], m1["alpha"].reshape(-1, order="F"))
