@@ -591,7 +591,7 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
         // chunk's voxel solve.  The host does not know the list's length, so
         // chunks past it launch and return at once.
         const int mpad = dk::tc_mpad(o.nTE), ntiles = dk::tc_ntiles(o.nRefAngles, n);
-        const long ldF = (long)ntiles * dk::kTcTileN;
+        const long ldF = 2L * ntiles * dk::kTcTileN;
         const long C = std::max<long>(dk::kTcTileM, std::min<long>(kTcChunk, V));
         void *F, *Fexp;
         if (int rc = buf(ctx, "tc_products", sizeof(float) * (size_t)C * ldF, &F)) return rc;
@@ -649,6 +649,23 @@ size_t layout_outputs(const decaes_t2map_opts &o, bool want_t2part, double *d, O
     om.sfr = pt; om.sgm = pt ? pt + V : nullptr; om.mfr = pt ? pt + 2 * V : nullptr; om.mgm = pt ? pt + 3 * V : nullptr;
     om.total = tot;
     return tot;
+}
+
+// Statistics of the tensor-core grid products of the last call (its stream
+// has completed): device time of the recorded launches, launches, and the
+// thread blocks that gave up a bounded wait (counter at byte 32 of cnt).
+void fill_tc_stats(decaes_ctx *ctx, const void *cnt) {
+    unsigned herr = 0;
+    if (ctx->tc_chunks > 0) cudaMemcpy(&herr, (const char *)cnt + 32, sizeof herr, cudaMemcpyDeviceToHost);
+    double gp = 0.0;
+    for (int q = 0; q < std::min(ctx->tc_chunks, kTcEvents); ++q) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ctx->tc_ev[2 * q], ctx->tc_ev[2 * q + 1]);
+        gp += t;
+    }
+    ctx->stats.ms_grid_products = gp;
+    ctx->stats.grid_product_launches = ctx->tc_chunks;
+    ctx->stats.grid_product_failures = (int32_t)herr;
 }
 
 int out_layout(decaes_ctx *ctx, const decaes_t2map_opts &o, bool want_t2part, OutMap &om) {
@@ -829,6 +846,7 @@ static int t2map_host(decaes_ctx *ctx, const decaes_t2map_opts *mo, const decaes
     cudaEventElapsedTime(&t, ctx->ev[4], ctx->ev[5]); S.ms_d2h = t;
     S.solve_launches = 1;
     S.kernel_launches = launches;
+    fill_tc_stats(ctx, cnt);
     return DECAES_OK;
 }
 
@@ -914,24 +932,15 @@ extern "C" int decaes_sync_stats(decaes_ctx *ctx, void *stream) {
     if (int rc = buf(ctx, "counters", 64, &cnt)) return rc;
     int hn;
     unsigned long long hs[2];
-    unsigned herr = 0;
     CK(cudaMemcpy(&hn, cnt, sizeof(int), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(hs, (char *)cnt + 16, sizeof hs, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(&herr, (char *)cnt + 32, sizeof herr, cudaMemcpyDeviceToHost));
     float t;
     ctx->stats.voxels_processed = hn;
     ctx->stats.nnls_cap_hits = (int64_t)hs[0];
     ctx->stats.search_limit_hits = (int64_t)hs[1];
     cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[5]); ctx->stats.ms_total = t;
     cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]); ctx->stats.ms_solve = t;
-    double gp = 0.0;
-    for (int q = 0; q < std::min(ctx->tc_chunks, kTcEvents); ++q) {
-        cudaEventElapsedTime(&t, ctx->tc_ev[2 * q], ctx->tc_ev[2 * q + 1]);
-        gp += t;
-    }
-    ctx->stats.ms_grid_products = gp;
-    ctx->stats.grid_product_launches = ctx->tc_chunks;
-    ctx->stats.grid_product_failures = herr;
+    fill_tc_stats(ctx, cnt);
     return DECAES_OK;
 }
 

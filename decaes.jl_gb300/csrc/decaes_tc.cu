@@ -8,17 +8,19 @@
 // GEMM: F[t, k*n + j] = sum_i A_k(i, j) y_t(i), M = voxels, N = K*n basis
 // columns, K-dimension = echoes.
 //
-// Precision: FP64 products are needed (the loss is compared between angles),
-// so each operand is split into S = 3 bf16 "slices" of a fixed-point value:
-//   v = s_0 2^-8 + s_1 2^-16 + s_2 2^-24 + r,   s_i integers, |s_0| <= 256,
-//   |s_1|, |s_2| <= 128, |r| <= 2^-25,
+// Precision: near-FP64 products are needed (the search compares losses
+// between angles, and an FP32-rounded A_k'b moved fitted angles by ~0.05 deg
+// at p99), so each operand is split into S = 4 bf16 "slices" of a
+// fixed-point value:
+//   v = s_0 2^-8 + s_1 2^-16 + s_2 2^-24 + s_3 2^-32 + r,  s_i integers,
+//   |s_0| <= 256, |s_1|, |s_2|, |s_3| <= 128, |r| <= 2^-33,
 // for v = y / 2^e (e the voxel's exponent: |v| < 1) and for the basis entries
 // (0 <= A <= 1).  Every s_i is exactly a bf16.  The slice products are grouped
 // by scale: D_d = sum_{s+t=d} sum_i s_s(i) a_t(i), d < S, each an integer
-// below 2^24 (m <= 128), so the FP32 accumulation of the tensor cores is exact;
-// F = sum_d D_d 2^-8(d+2) then carries ~2^-24 relative error from the dropped
-// slice pairs and one FP32 rounding: split-precision bf16 with FP32
-// accumulation, exact up to the truncation.
+// below 2^24 (m <= 128), so the FP32 accumulation of the tensor cores is
+// exact; F = sum_d D_d 2^-8(d+2) is formed exactly as a float pair (hi, lo)
+// and carries ~2^-32 relative error from the dropped slice pairs: split-
+// precision bf16 with FP32 accumulation, exact up to the truncation.
 //
 // Layout and flow (one CTA of 4 warps, persistent over 128-voxel tiles):
 //   * the CTA gathers its voxels' echo trains from the image, forms e and the
@@ -33,7 +35,7 @@
 //     accumulators D_0..D_{S-1} in TMEM columns [64d, 64d + 64)) and commits
 //     them to an mbarrier;
 //   * the four warps read their 32 TMEM lanes (one voxel each) with
-//     tcgen05.ld, combine the D_d in FP32 and store 64 floats per voxel.
+//     tcgen05.ld, sum the D_d as float pairs and store 64 pairs per voxel.
 // Every mbarrier wait is bounded; a CTA that gives up records it in the error
 // counter, marks its voxels' rows unusable (the voxel kernel then forms those
 // products itself), waits for its own operations still in flight and frees
@@ -127,7 +129,14 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Fixed-point slices of v (|v| <= 1): v = s0 2^-8 + s1 2^-16 + s2 2^-24 (+ r).
+// s + e = a + b exactly (Knuth's two-sum; the build does not contract).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// Fixed-point slices of v (|v| <= 1): v = sum_i s_i 2^-8(i+1) (+ r).
 __device__ __forceinline__ void slices_of(double v, float *s) {
     double t = v * 256.0;
 #pragma unroll
@@ -169,9 +178,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_grid_products(const __grid_co
     const int tid = threadIdx.x, warp = tid >> 5;
     const int mpad = p.mpad;
     const unsigned aSlice = tc_slice_bytes(kTcTileM, mpad), bSlice = tc_slice_bytes(kTcTileN, mpad);
+    const int nbuf = tc_nbuf(mpad);
     unsigned char *sA = sm;
-    unsigned char *sB = sA + kS * aSlice;  // two buffers of kS slices
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sB + 2 * kS * bSlice);  // [0], [1] basis tiles, [2] MMA done
+    unsigned char *sB = sA + kS * aSlice;  // nbuf buffers of kS slices
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sB + nbuf * kS * bSlice);  // [0], [1] basis tiles, [2] MMA done
     uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 4);
     if (tid == 0) {
         mbar_init(&bar[0], 1);
@@ -241,10 +251,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_grid_products(const __grid_co
         }
         #pragma unroll 1
         for (int nt = 0; nt < p.ntiles; ++nt) {
-            const int buf = nt & 1;
+            const int buf = nbuf == 2 ? (nt & 1) : 0;
             unsigned char *sBb = sB + buf * tileBytes;
             if (tid == 0) {
-                if (nt + 1 < p.ntiles) {  // the other buffer's MMAs completed in the previous round
+                if (nbuf == 1 && nt > 0) {  // one buffer: its previous tile's MMAs completed last round
+                    mbar_expect_tx(&bar[0], tileBytes);
+                    bulk_g2s(sB, p.Bsl + (size_t)nt * tileBytes, tileBytes, &bar[0]);
+                    pendB0 = true;
+                }
+                if (nbuf == 2 && nt + 1 < p.ntiles) {  // the other buffer's MMAs completed in the previous round
                     uint64_t *nb = &bar[buf ^ 1];
                     mbar_expect_tx(nb, tileBytes);
                     bulk_g2s(sB + (buf ^ 1) * tileBytes, p.Bsl + (size_t)(nt + 1) * tileBytes, tileBytes, nb);
@@ -296,18 +311,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_grid_products(const __grid_co
                 for (int q = 0; q < kS; ++q) tmem_ld32(tmem + lane_base + (uint32_t)(q * kTcTileN + 32 * h), d[q]);
                 tmem_wait_ld();
                 if (t < nv) {
-                    float4 *dst = reinterpret_cast<float4 *>(p.F + (t - p.t0) * p.ldF + (long)nt * kTcTileN + 32 * h);
+                    float4 *dst =
+                        reinterpret_cast<float4 *>(p.F + (t - p.t0) * p.ldF + 2 * ((long)nt * kTcTileN + 32 * h));
 #pragma unroll
-                    for (int c4 = 0; c4 < 8; ++c4) {
+                    for (int c2 = 0; c2 < 16; ++c2) {
                         float o[4];
 #pragma unroll
-                        for (int c = 0; c < 4; ++c) {
-                            float acc = d[kS - 1][4 * c4 + c];
+                        for (int c = 0; c < 2; ++c) {
+                            // sum_d D_d 2^-8(d+2): every term exact in FP32, summed as a float pair
+                            const int col = 2 * c2 + c;
+                            float s = d[0][col] * 1.52587890625e-05f, e = 0.f, r;  // 2^-16
+                            float sc = 1.52587890625e-05f;
 #pragma unroll
-                            for (int q = kS - 2; q >= 0; --q) acc = fmaf(acc, 0.00390625f, d[q][4 * c4 + c]);
-                            o[c] = acc * 1.52587890625e-05f;  // 2^-16
+                            for (int q = 1; q < kS; ++q) {
+                                sc *= 0.00390625f;
+                                two_sum(s, d[q][col] * sc, s, r);
+                                e += r;
+                            }
+                            const float hi = s + e;
+                            o[2 * c] = hi;
+                            o[2 * c + 1] = e - (hi - s);
                         }
-                        dst[c4] = make_float4(o[0], o[1], o[2], o[3]);
+                        dst[c2] = make_float4(o[0], o[1], o[2], o[3]);
                     }
                 }
             }
@@ -334,7 +359,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_grid_products(const __grid_co
 }
 
 size_t tc_smem_bytes(int mpad) {
-    return (size_t)kS * tc_slice_bytes(kTcTileM, mpad) + 2u * kS * tc_slice_bytes(kTcTileN, mpad) + 64;
+    return (size_t)kS * tc_slice_bytes(kTcTileM, mpad) + (size_t)tc_nbuf(mpad) * kS * tc_slice_bytes(kTcTileN, mpad) + 64;
 }
 
 cudaError_t tc_make_basis_slices(const double *As, int m, int n, int K, unsigned char *out, cudaStream_t st) {

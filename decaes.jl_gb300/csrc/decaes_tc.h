@@ -9,7 +9,7 @@ namespace dk {
 
 constexpr int kTcTileM = 128;    // voxels per tile (MMA M)
 constexpr int kTcTileN = 64;     // grid-basis columns per tile (MMA N)
-constexpr int kTcSlices = 3;     // bf16 fixed-point slices per operand
+constexpr int kTcSlices = 4;     // bf16 fixed-point slices per operand
 constexpr int kTcThreads = 128;  // four warps: one TMEM lane quarter each
 constexpr int kTcTmemCols = 256; // TMEM columns per CTA (kTcSlices x kTcTileN used)
 
@@ -35,12 +35,19 @@ struct TcParams {
     long t0, t1;                   // the list positions of this launch, [t0, min(t1, *nvox))
     const unsigned char *Bsl;      // grid-basis slices: ntiles blocks of kTcSlices x 64 x mpad bf16
     int ntiles;
-    float *F;                      // F[(t - t0) * ldF + k*n + j], scaled by 2^-e of the voxel
-    long ldF;                      // ntiles * 64
+    float *F;                      // F[(t - t0) * ldF + 2 (k*n + j) + {0, 1}]: the product as a float pair
+                                   // (hi, lo), scaled by 2^-e of the voxel
+    long ldF;                      // 2 * ntiles * 64
     int *Fexp;                     // per position: e, or INT_MIN when the voxel's row is not usable
     unsigned *err;                 // CTAs whose bounded waits gave up
 };
 
+// Basis-tile buffers of one CTA: two when they fit beside the voxel tile in
+// the 227 KB of shared memory a block may use, else one.
+__host__ __device__ inline int tc_nbuf(int mpad) {
+    const unsigned two = kTcSlices * tc_slice_bytes(kTcTileM, mpad) + 2u * kTcSlices * tc_slice_bytes(kTcTileN, mpad) + 64u;
+    return two <= 227u * 1024u ? 2 : 1;
+}
 // Shared memory of one CTA of k_grid_products (before the 100 KB floor).
 size_t tc_smem_bytes(int mpad);
 // Grid-basis slices (tc_ntiles(K, n) * kTcSlices * tc_slice_bytes(64, mpad)

@@ -131,13 +131,17 @@ static __device__ __noinline__ void gram_rhs_t(GramWS &g, const double *AT, int 
     __syncwarp();
 }
 
-// f = A'b from a precomputed row of products in FP32 (the tensor-core grid
-// products of the voxel), times their scale to the normalized decay.
+// f = A'b from a precomputed row of products held as float pairs (hi, lo)
+// (the tensor-core grid products of the voxel), times their scale to the
+// normalized decay.
 static __device__ __noinline__ void gram_rhs_f32(GramWS &g, const float *F, int n, double scale, int m,
                                                  const double *b) {
     const int lane = threadIdx.x & 31;
     #pragma unroll 1
-    for (int j = lane; j < n; j += 32) g.f[j] = widen(__ldg(F + j)) * scale;
+    for (int j = lane; j < n; j += 32) {
+        const float2 v = __ldg(reinterpret_cast<const float2 *>(F) + j);
+        g.f[j] = (widen(v.x) + widen(v.y)) * scale;
+    }
     gram_bb(g, m, b);
     __syncwarp();
 }

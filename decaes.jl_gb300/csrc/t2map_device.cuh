@@ -907,7 +907,7 @@ static __device__ void fa_update(Search &S, int I) {
         // precomputed Gram matrix of grid basis I; A'b from its transposed copy
         gram_load(w.g, P.Gs + (long)(I - 1) * (n * (n + 1) / 2), n);
         if (w.fk_ok)  // from the tensor-core grid products
-            gram_rhs_f32(w.g, P.Fk + w.slot * P.ldF + (long)(I - 1) * n, n, w.fscale, m, w.data);
+            gram_rhs_f32(w.g, P.Fk + w.slot * P.ldF + 2L * (I - 1) * n, n, w.fscale, m, w.data);
         else
             gram_rhs_t(w.g, P.AsT + (long)(I - 1) * m * n, m, n, w.data);
         r = gram_nnls(w.g, w.s.x, w.s.w, w.s.idx, n, 0.0, 3 * n, &w.g.lastk);

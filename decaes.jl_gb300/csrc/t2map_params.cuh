@@ -44,7 +44,8 @@ struct Params {
     // the voxel-list positions of this launch: [tq0, min(tq1, *nvox)); tq1 <= 0: to the end
     long tq0, tq1;
     // tensor-core grid products (DECAES_PREC_MIXED_TC): row t - tq0 of F holds
-    // A_k' y for every grid angle, scaled by 2^-Fexp[t - tq0] (INT_MIN: unusable)
+    // A_k' y for every grid angle as float pairs (hi, lo), scaled by
+    // 2^-Fexp[t - tq0] (INT_MIN: unusable)
     const float *Fk;
     const int *Fexp;
     long ldF;
