@@ -690,21 +690,22 @@ def main():
         line["mixed_vs_fp64"]["gate_met"] = bool(e["mwf_abs"]["p99"] <= 1e-3 and e["same_processed_voxels"])
 
     if tc is not None:
-        # the grid-product GEMM's work: 2 x 6 slice-pair products x K*nT2 x nTE per voxel
+        # the grid-product GEMM's work: 2 x 10 slice-pair products x K*nT2 x nTE per voxel
         w_ = WORKLOADS[args.workload]
-        gemm_flops = 2.0 * 6 * w_["K"] * w_["nT2"] * (-(-w_["nTE"] // 16) * 16) * Vp
-        gemm_bytes = (w_["K"] * w_["nT2"] * 4.0 + 4.0 + 4.0 * w_["nTE"]) * Vp
+        gemm_flops = 2.0 * 10 * w_["K"] * w_["nT2"] * (-(-w_["nTE"] // 16) * 16) * Vp
+        gemm_bytes = (w_["K"] * w_["nT2"] * 8.0 + 4.0 + 4.0 * w_["nTE"]) * Vp
         line["tensor_core_grid_products"] = {
             "method": "mixed_tc: the search's A_k'b for every grid angle from one tcgen05 GEMM per 2^19 voxels "
-                      "(3 bf16 fixed-point slices per operand, exact FP32 accumulation), read by the voxel kernel",
+                      "(4 bf16 fixed-point slices per operand, exact FP32 accumulation, float-pair products), "
+                      "read by the voxel kernel",
             "value": tc["value"], "ms_per_step": tc["ms_per_step"], "steps": tc["steps"],
             "speedup_vs_mixed": ms_per_step / tc["ms_per_step"],
             "gemm_ms_per_step": tc["grid_products_ms"], "gemm_launches": tc["grid_product_launches"],
             "gemm_failures": tc["grid_product_failures"],
             "gemm_tflops": gemm_flops / (tc["grid_products_ms"] * 1e-3) / 1e12 if tc["grid_products_ms"] else None,
             "gemm_gbs": gemm_bytes / (tc["grid_products_ms"] * 1e-3) / 1e9 if tc["grid_products_ms"] else None,
-            "gemm_work": "2 x 6 slice-pair products x K*nT2 x nTE(padded to 16) per above-threshold voxel; "
-                         "bytes = K*nT2 FP32 products + exponent + the FP32 echo train per voxel",
+            "gemm_work": "2 x 10 slice-pair products x K*nT2 x nTE(padded to 16) per above-threshold voxel; "
+                         "bytes = K*nT2 float-pair products + exponent + the FP32 echo train per voxel",
         }
         if fp64 is not None:
             line["tensor_core_grid_products"]["errors_vs_fp64"] = method_errors(

@@ -139,6 +139,7 @@ __global__ void __launch_bounds__(128) k_voxels_legacy(const __grid_constant__ P
 __global__ void __launch_bounds__(128) k_voxels_batch_legacy(const __grid_constant__ BatchParams B);
 __global__ void __launch_bounds__(256) k_voxels_plain(const __grid_constant__ Params P);
 __global__ void __launch_bounds__(128) k_voxels_mixed(const __grid_constant__ Params P);
+__global__ void __launch_bounds__(128) k_voxels_mixed_tc(const __grid_constant__ Params P);
 __global__ void __launch_bounds__(128) k_voxels_batch_plain(const __grid_constant__ BatchParams B);
 __global__ void __launch_bounds__(128) k_voxels_batch_mixed(const __grid_constant__ BatchParams B);
 
@@ -576,7 +577,9 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
     P.smem_stride = wsm;
     int wpb = tuned_wpb(ctx, o), grid = 0;
     size_t smem = 0;
-    auto kern = o.legacy ? dk::k_voxels_legacy : (is_mixed(o) ? dk::k_voxels_mixed : dk::k_voxels_plain);
+    const bool tc = o.precision == DECAES_PREC_MIXED_TC && P.angle_mode == 0 && !o.legacy;
+    auto kern = o.legacy ? dk::k_voxels_legacy
+                         : (tc ? dk::k_voxels_mixed_tc : (is_mixed(o) ? dk::k_voxels_mixed : dk::k_voxels_plain));
     // the plain method's large workspace: blocks of up to 8 warps can hold a
     // warp per SM more than single-warp blocks (its kernel allows 256 threads)
     if (kern == dk::k_voxels_plain && tuned_wpb_or0(ctx, o) == 0) wpb = most_warps_wpb(ctx, kern, wsm, 8);
@@ -585,7 +588,7 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
     if (int rc = buf(ctx, "scratch", sizeof(double) * (size_t)P.scr_stride * grid * wpb, &scr)) return rc;
     P.scratch = (double *)scr;
     ctx->tc_chunks = 0;
-    if (o.precision == DECAES_PREC_MIXED_TC && P.angle_mode == 0) {
+    if (tc) {
         // The search's grid products on the tensor cores, a chunk of the voxel
         // list at a time (bounded F buffer): products of the chunk, then the
         // chunk's voxel solve.  The host does not know the list's length, so

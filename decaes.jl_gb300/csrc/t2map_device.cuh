@@ -23,11 +23,18 @@
 #ifndef DECAES_METHODS
 #define DECAES_METHODS 3
 #endif
+// DECAES_TC_PRODUCTS=1: the kernel reads the flip-angle search's grid
+// products from the tensor-core GEMM (DECAES_PREC_MIXED_TC); only its own
+// translation unit compiles that path, so the other kernels are unchanged.
+#ifndef DECAES_TC_PRODUCTS
+#define DECAES_TC_PRODUCTS 0
+#endif
 
 namespace dk {
 
 constexpr bool kLegacyKernel = DECAES_LEGACY_KERNEL != 0;
 constexpr bool kHasPlain = (DECAES_METHODS & 1) != 0, kHasMixed = (DECAES_METHODS & 2) != 0;
+constexpr bool kTcProducts = DECAES_TC_PRODUCTS != 0;
 
 // Helpers with several call sites on the mixed method's hot path are kept out
 // of line in its single-method kernel (one copy in the instruction cache
@@ -55,9 +62,6 @@ struct Warp {
     float *As32;   // FP32 basis staged in shared memory, column-major, leading dimension ldA
     int ldA;
     bool mixed;    // the mixed method (Params::mixed)
-    long slot;     // the voxel's position in this launch's part of the voxel list
-    bool fk_ok;    // its tensor-core grid products are usable
-    double fscale; // and their scale to the normalized decay: 2^e / max
 };
 // The warp's method, folded to a constant in single-method kernels.
 __device__ __forceinline__ bool use_mixed(const Warp &w) { return kHasMixed && (!kHasPlain || w.mixed); }
@@ -893,6 +897,10 @@ struct Search {
     int *sidx;            // sorted evaluated indices, 1-based (K)
     unsigned seen[8];     // bitset over <= 256 grid points (warp-uniform registers)
     int npts, numeval, mineval, maxeval;
+#if DECAES_TC_PRODUCTS
+    const float *Frow;    // the voxel's tensor-core grid products (float pairs), or null
+    double fscale;        // their scale to the normalized decay: 2^e / max
+#endif
 };
 __device__ __forceinline__ bool sseen(const Search &S, int I) { return (S.seen[(I - 1) >> 5] >> ((I - 1) & 31)) & 1u; }
 
@@ -906,9 +914,11 @@ static __device__ void fa_update(Search &S, int I) {
     if (use_mixed(w)) {
         // precomputed Gram matrix of grid basis I; A'b from its transposed copy
         gram_load(w.g, P.Gs + (long)(I - 1) * (n * (n + 1) / 2), n);
-        if (w.fk_ok)  // from the tensor-core grid products
-            gram_rhs_f32(w.g, P.Fk + w.slot * P.ldF + 2L * (I - 1) * n, n, w.fscale, m, w.data);
+#if DECAES_TC_PRODUCTS
+        if (S.Frow)  // from the tensor-core grid products
+            gram_rhs_f32(w.g, S.Frow + 2L * (I - 1) * n, n, S.fscale, m, w.data);
         else
+#endif
             gram_rhs_t(w.g, P.AsT + (long)(I - 1) * m * n, m, n, w.data);
         r = gram_nnls(w.g, w.s.x, w.s.w, w.s.idx, n, 0.0, 3 * n, &w.g.lastk);
     } else {
@@ -1080,10 +1090,19 @@ static __device__ void fa_min_bbox(const Search &S, double x, int &plo, int &phi
     phi = hi;
 }
 // optimize_flip_angle!, src/T2mapSEcorr.jl:409-423 + bisection_search, src/splines.jl:750-775
-static __device__ double flip_angle_search(Warp &w) {
+// slot: the voxel's position in this launch's part of the voxel list (its
+// row of tensor-core grid products in the kernels that read them)
+static __device__ double flip_angle_search(Warp &w, double mx, long slot) {
     const Params &P = *w.P;
     Search S;
     S.w = &w;
+#if DECAES_TC_PRODUCTS
+    {
+        const int e = P.Fexp[slot];
+        S.Frow = e != INT_MIN ? P.Fk + slot * P.ldF : nullptr;
+        S.fscale = e != INT_MIN ? ldexp(1.0, e) / (mx > 0 ? mx : 1.0) : 0.0;
+    }
+#endif
     S.u = w.scr + (long)P.m * P.n;
     S.du = S.u + P.K;
     S.sidx = reinterpret_cast<int *>(S.du + P.K);
@@ -1175,7 +1194,7 @@ static __device__ void warp_basis_f32(Warp &w, double alpha) {
 // ----------------------------------------------------------------------------
 // One voxel (src/T2mapSEcorr.jl:201-238, save_results! 512-591, T2part 95-138)
 // ----------------------------------------------------------------------------
-static __device__ void process_voxel(Warp &w, long v) {
+static __device__ void process_voxel(Warp &w, long v, long slot = 0) {
     const Params &P = *w.P;
     const int m = P.m, n = P.n, lane = w.lane;
     w.nsol = 0;
@@ -1198,12 +1217,6 @@ static __device__ void process_voxel(Warp &w, long v) {
         #pragma unroll 1
         for (int i = lane; i < m; i += 32) w.data[i] = w.data[i] / mx;
     __syncwarp();
-    w.fk_ok = false;
-    if (use_mixed(w) && P.Fk) {
-        const int e = P.Fexp[w.slot];
-        w.fk_ok = e != INT_MIN;
-        w.fscale = w.fk_ok ? ldexp(1.0, e) / (mx > 0 ? mx : 1.0) : 0.0;
-    }
 
     double alpha;
     w.g.lastk = 0;  // warm starts never cross voxels (results independent of scheduling)
@@ -1215,7 +1228,7 @@ static __device__ void process_voxel(Warp &w, long v) {
         if (P.angle_mode == 2) {
             alpha = P.image_f32 ? (double)static_cast<const float *>(P.b1map)[v] : static_cast<const double *>(P.b1map)[v];
         } else {
-            alpha = flip_angle_search(w);
+            alpha = flip_angle_search(w, mx, slot);
         }
         if (use_mixed(w)) warp_basis_f32(w, alpha);
         else warp_basis(w, alpha, w.A);

@@ -41,7 +41,7 @@ struct Params {
     const double *AsT;  // the grid (or fixed) bases transposed, K x m x n (row-major per basis)
     int epg_lanes_f32;  // lanes of the FP32 EPG (states in the Gram and factor regions)
     long smem_stride;   // doubles of shared memory per warp (several warps per block)
-    // the voxel-list positions of this launch: [tq0, min(tq1, *nvox)); tq1 <= 0: to the end
+    // the voxel-list positions of a k_voxels_mixed_tc launch: [tq0, min(tq1, *nvox))
     long tq0, tq1;
     // tensor-core grid products (DECAES_PREC_MIXED_TC): row t - tq0 of F holds
     // A_k' y for every grid angle as float pairs (hi, lo), scaled by

@@ -76,6 +76,8 @@ __device__ __forceinline__ void voxels_body(const Params &P) {
     w.nnls_caps = 0;
     w.loop_caps = 0;
     warp_setup(w, P, smem + (long)wib * P.smem_stride, P.scratch + ((long)blockIdx.x * wpb + wib) * P.scr_stride);
+#if DECAES_TC_PRODUCTS
+    // one chunk of the voxel list: positions [tq0, min(tq1, *nvox))
     const long nvox = P.tq1 > 0 && P.tq1 < (long)*P.nvox ? P.tq1 : (long)*P.nvox;
     for (;;) {
         int q = 0;
@@ -83,9 +85,18 @@ __device__ __forceinline__ void voxels_body(const Params &P) {
         q = __shfl_sync(FULL, q, 0);
         const long t = P.tq0 + q;
         if (t >= nvox) break;
-        w.slot = q;
+        process_voxel(w, (long)P.vidx[t], q);
+    }
+#else
+    const int nvox = *P.nvox;
+    for (;;) {
+        int t = 0;
+        if (w.lane == 0) t = atomicAdd(P.counter, 1);
+        t = __shfl_sync(FULL, t, 0);
+        if (t >= nvox) break;
         process_voxel(w, (long)P.vidx[t]);
     }
+#endif
     if (w.lane == 0) {
         if (w.nnls_caps) atomicAdd(&P.stats[0], (unsigned long long)w.nnls_caps);
         if (w.loop_caps) atomicAdd(&P.stats[1], (unsigned long long)w.loop_caps);
@@ -135,7 +146,6 @@ __device__ __forceinline__ void voxels_batch_body(const BatchParams &B) {
             warp_setup(w, *Pw, ws, scr);
             cur = lo;
         }
-        w.slot = t - B.offsets[lo];
         process_voxel(w, (long)Pw->vidx[t - B.offsets[lo]]);
     }
     if (cur >= 0 && w.lane == 0) {

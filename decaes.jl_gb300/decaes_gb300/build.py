@@ -23,7 +23,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-Xptxas", "-v"] + ARCH
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
-SOURCES_CU = ["decaes_gpu.cu", "decaes_plain.cu", "decaes_mixed.cu", "decaes_legacy.cu", "decaes_noalloc.cu", "decaes_tc.cu"]
+SOURCES_CU = ["decaes_gpu.cu", "decaes_plain.cu", "decaes_mixed.cu", "decaes_legacy.cu", "decaes_noalloc.cu", "decaes_tc.cu",
+              "decaes_mixed_tc.cu"]
 SOURCES_CPP = ["host.cpp"]
 
 
