@@ -382,83 +382,118 @@ def fp64_peak_tflops(torch):
     return 2 * n ** 3 / (best * 1e-3) / 1e12
 
 
-def run_batch_workload(args):
-    """The batched uneven workload: many volumes of different shapes solved by
-    one graph replay of a prepared batch (a persistent launch per occupancy
-    class), against the same volumes solved one device call after another."""
-    import torch
-    import decaes_gb300 as D
-    from decaes_gb300 import _lib
-    rng = np.random.default_rng(args.seed)
-    nvol = args.nvol
-    vols, specs = [], []
-    V_tot = 0
+def batch_volume_specs(rng, nvol, seed):
+    """Volume shapes and options of the uneven-batch configuration: XY ~U{64..240
+    step 16}, Z ~U{32..48}, nTE ~U{24..64}, TE ~U(5,12) ms, nT2 in {40,48,60},
+    background (mask) fraction ~U(0.3,0.6), chi2 and none alternating."""
+    out = []
     for i in range(nvol):
-        X = (int(rng.choice(np.arange(64, 241, 16))), int(rng.choice(np.arange(64, 241, 16))), int(rng.integers(1, 4)))
+        X = (int(rng.choice(np.arange(64, 241, 16))), int(rng.choice(np.arange(64, 241, 16))), int(rng.integers(32, 49)))
         m, n = int(rng.integers(24, 65)), int(rng.choice([40, 48, 60]))
         TE, bg = float(rng.uniform(5e-3, 12e-3)), float(rng.uniform(0.3, 0.6))
-        reg = "chi2" if i % 2 == 0 else "none"
-        mo = D.T2mapOptions(MatrixSize=X, nTE=m, TE=TE, nT2=n, T2Range=(10e-3, 2.0), Reg=reg, nRefAngles=32,
-                            Chi2Factor=1.02 if reg == "chi2" else None, Threshold=THRESHOLD, precision=args.precision)
-        po = D.T2partOptions.from_t2map(mo, SPWin=SPWIN, MPWin=MPWIN)
-        img = D.mock_image(D.MockImageOptions(MatrixSize=X, nTE=m, TE=TE, BackgroundFraction=bg), seed=args.seed + i,
-                           dtype=np.float32)
-        d_img = torch.from_numpy(img.reshape(-1, order="F").copy()).cuda()
-        V = int(np.prod(X))
-        V_tot += V
-        out = {"dist": torch.empty(V * n, dtype=torch.float32, device="cuda")}
-        for k in ("gdn", "ggm", "gva", "fnr", "snr", "alpha", "sfr", "sgm", "mfr", "mgm"):
-            out[k] = torch.empty(V, dtype=torch.float32, device="cuda")
-        mc = _lib.T2mapOutC(**{k: out[k].data_ptr() for k in ("dist", "gdn", "ggm", "gva", "fnr", "snr", "alpha")})
-        pc = _lib.T2partOutC(**{k: out[k].data_ptr() for k in ("sfr", "sgm", "mfr", "mgm")})
-        vols.append(_lib.VolumeC(mopts=mo.to_c(), popts=po.to_c(), has_t2part=1, dtype=_lib.F32,
-                                 d_image=d_img.data_ptr(), d_b1map=None, d_mout=mc, d_pout=pc))
-        specs.append((mo, po, d_img, out, mc, pc))
-    ctx = D.Context(0)
+        out.append(dict(X=X, m=m, n=n, TE=TE, bg=bg, reg="chi2" if i % 2 == 0 else "none", seed=seed + i))
+    return out
+
+
+def run_batch_groups(ctx, torch, specs, precision, group, steps, warmup, compare_groups):
+    """The volumes in groups of `group`: each group is prepared once
+    (decaes_batch_create: validation, buffers, resident bases, captured graph),
+    replayed `warmup` times untimed and `steps` times timed with CUDA events on
+    its stream, then released before the next group, so device memory holds
+    one group at a time.  For the first `compare_groups` groups the same
+    volumes are also run as one device call each (timed the same way) and the
+    outputs compared.  Returns (voxels, processed voxels, batch ms per pass,
+    sequential ms of the compared groups, their voxels, same outputs)."""
+    import decaes_gb300 as D
+    from decaes_gb300 import _lib
     L = ctx.L
-    arr = (_lib.VolumeC * nvol)(*vols)
-    b = L.decaes_batch_create(ctx.h, arr, nvol)
-    if not b:
-        raise RuntimeError(L.decaes_last_error(ctx.h).decode())
-    stream = torch.cuda.Stream()  # an explicit stream: the events below see exactly the batch's work
-    for _ in range(args.warmup):
-        L.decaes_batch_run(b, C.c_void_p(stream.cuda_stream))
-    torch.cuda.synchronize()
-    clk = Clocks(0)
+    stream = torch.cuda.Stream()  # an explicit stream: the events see exactly the batch's work
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with clk:
+    V_tot, ms_tot, ms_seq, V_seq, same, Vp = 0, 0.0, 0.0, 0, True, 0
+    for g0 in range(0, len(specs), group):
+        vols, keep = [], []
+        for sp in specs[g0:g0 + group]:
+            mo = D.T2mapOptions(MatrixSize=sp["X"], nTE=sp["m"], TE=sp["TE"], nT2=sp["n"], T2Range=(10e-3, 2.0),
+                                Reg=sp["reg"], nRefAngles=32, Chi2Factor=1.02 if sp["reg"] == "chi2" else None,
+                                Threshold=THRESHOLD, precision=precision)
+            po = D.T2partOptions.from_t2map(mo, SPWin=SPWIN, MPWin=MPWIN)
+            img = D.mock_image(D.MockImageOptions(MatrixSize=sp["X"], nTE=sp["m"], TE=sp["TE"], BackgroundFraction=sp["bg"]),
+                               seed=sp["seed"], dtype=np.float32)
+            Vp += int((img[..., 0] > THRESHOLD).sum())
+            d_img = torch.from_numpy(img.reshape(-1, order="F").copy()).cuda()
+            V = int(np.prod(sp["X"]))
+            V_tot += V
+            out = {"dist": torch.empty(V * sp["n"], dtype=torch.float32, device="cuda")}
+            for k in ("gdn", "ggm", "gva", "fnr", "snr", "alpha", "sfr", "sgm", "mfr", "mgm"):
+                out[k] = torch.empty(V, dtype=torch.float32, device="cuda")
+            mc = _lib.T2mapOutC(**{k: out[k].data_ptr() for k in ("dist", "gdn", "ggm", "gva", "fnr", "snr", "alpha")})
+            pc = _lib.T2partOutC(**{k: out[k].data_ptr() for k in ("sfr", "sgm", "mfr", "mgm")})
+            vols.append(_lib.VolumeC(mopts=mo.to_c(), popts=po.to_c(), has_t2part=1, dtype=_lib.F32,
+                                     d_image=d_img.data_ptr(), d_b1map=None, d_mout=mc, d_pout=pc))
+            keep.append((mo, po, d_img, out, mc, pc, V))
+        arr = (_lib.VolumeC * len(vols))(*vols)
+        b = L.decaes_batch_create(ctx.h, arr, len(vols))
+        if not b:
+            raise RuntimeError(L.decaes_last_error(ctx.h).decode())
+        for _ in range(warmup):
+            L.decaes_batch_run(b, C.c_void_p(stream.cuda_stream))
+        torch.cuda.synchronize()
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             L.decaes_batch_run(b, C.c_void_p(stream.cuda_stream))
         e1.record(stream)
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
-    sfr_batch = [sp[3]["sfr"].double().cpu().numpy() for sp in specs]
-    L.decaes_batch_destroy(b)
-    # the same volumes, one device call each
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for mo, po, d_img, out, mc, pc in specs:
-        ctx.check(L.decaes_t2map_t2part_device(ctx.h, C.byref(mo.to_c()), C.byref(po.to_c()), C.c_void_p(d_img.data_ptr()),
-                                               _lib.F32, None, C.byref(mc), C.byref(pc), C.c_void_p(stream.cuda_stream)))
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms_seq = e0.elapsed_time(e1)
-    same = all(np.array_equal(np.nan_to_num(a, nan=-1), np.nan_to_num(sp[3]["sfr"].double().cpu().numpy(), nan=-1))
-               for a, sp in zip(sfr_batch, specs))
+        ms_tot += e0.elapsed_time(e1) / steps
+        L.decaes_batch_destroy(b)
+        if g0 // group < compare_groups:
+            sfr_batch = [k[3]["sfr"].double().cpu().numpy() for k in keep]
+            e0.record(stream)
+            for mo, po, d_img, out, mc, pc, V in keep:
+                ctx.check(L.decaes_t2map_t2part_device(ctx.h, C.byref(mo.to_c()), C.byref(po.to_c()),
+                                                       C.c_void_p(d_img.data_ptr()), _lib.F32, None, C.byref(mc),
+                                                       C.byref(pc), C.c_void_p(stream.cuda_stream)))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms_seq += e0.elapsed_time(e1)
+            V_seq += sum(k[6] for k in keep)
+            same = same and all(np.array_equal(np.nan_to_num(a, nan=-1), np.nan_to_num(k[3]["sfr"].double().cpu().numpy(), nan=-1))
+                                for a, k in zip(sfr_batch, keep))
+        del vols, keep, arr
+        torch.cuda.empty_cache()
+    return V_tot, Vp, ms_tot, ms_seq, V_seq, same
+
+
+BATCH_DESC = ("volumes: XY ~U{{64..240 step 16}}, Z ~U{{32..48}} (the 64x64x32..240x240x48 range), nTE ~U{{24..64}}, "
+              "TE ~U(5,12) ms, nT2 in {{40,48,60}}, mask ~U(0.3,0.6), Reg alternating chi2/none, 32 angles, Float32, "
+              "T2part fused")
+
+
+def run_batch_workload(args):
+    """The batched uneven workload at its stated sizes: many volumes of
+    different shapes, each group solved by one graph replay of a prepared
+    batch (a persistent launch per occupancy class), against the same volumes
+    solved one device call after another."""
+    import torch
+    import decaes_gb300 as D
+    rng = np.random.default_rng(args.seed)
+    specs = batch_volume_specs(rng, args.nvol, args.seed)
+    ctx = D.Context(0, hbm_budget_bytes=200 << 30)
+    clk = Clocks(0)
+    with clk:
+        V_tot, Vp, ms, ms_seq, V_seq, same = run_batch_groups(ctx, torch, specs, args.precision, args.group, args.steps,
+                                                              args.warmup, args.compare_groups)
     line = {
-        "metric": f"voxels/s, {nvol} uneven volumes in one graph replay (a persistent launch per occupancy class)",
+        "metric": f"voxels/s, {args.nvol} uneven volumes, each group of {args.group} in one graph replay "
+                  f"(a persistent launch per occupancy class)",
         "value": V_tot / (ms * 1e-3), "unit": "voxels/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f64+f32",
         "data": "synthetic (seeded 3-compartment EPG + Rician noise per volume)",
-        "config": {"workload": f"{nvol} volumes: XY ~U{{64..240 step 16}}, Z ~U{{1..3}} (the z-extent of the "
-                               f"64x64x32..240x240x48 range scaled down to fit one bench step), nTE ~U{{24..64}}, "
-                               f"TE ~U(5,12) ms, nT2 in {{40,48,60}}, mask ~U(0.3,0.6), Reg alternating chi2/none, "
-                               f"32 angles, Float32, T2part fused",
-                   "precision": args.precision, "voxels": V_tot},
-        "sequential_device_calls": {"value": V_tot / (ms_seq * 1e-3), "ms": ms_seq,
-                                    "speedup_of_batch": ms_seq / ms, "same_outputs": bool(same)},
+        "config": {"workload": f"{args.nvol} " + BATCH_DESC.replace("{{", "{").replace("}}", "}"),
+                   "precision": args.precision, "voxels": V_tot, "voxels_above_threshold": Vp, "group": args.group},
+        "sequential_device_calls": {"groups_compared": args.compare_groups, "voxels": V_seq,
+                                    "value": V_seq / (ms_seq * 1e-3) if ms_seq else None, "ms": ms_seq,
+                                    "same_outputs": bool(same)},
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -554,6 +589,9 @@ def main():
     ap.add_argument("--workload", default="lcurve48", choices=sorted(WORKLOADS) + ["batch", "serve"],
                     help="lcurve48 (headline), gcv56, chi2k8_48, batch (uneven volumes in one launch), serve")
     ap.add_argument("--nvol", type=int, default=256, help="volumes of --workload batch")
+    ap.add_argument("--group", type=int, default=32, help="volumes per prepared batch (--workload batch)")
+    ap.add_argument("--compare-groups", type=int, default=1,
+                    help="groups also run as one device call per volume (--workload batch)")
     ap.add_argument("--rates", default="0.5,1,2", help="arrival rates (requests/s) of --workload serve")
     ap.add_argument("--requests", type=int, default=40, help="requests per rate of --workload serve")
     ap.add_argument("--tick-voxels", type=int, default=262144, help="voxels per server tick (--workload serve)")
@@ -567,6 +605,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=None,
                     help="above-threshold voxels the CPU oracle runs on for cpu_baseline and parity")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the bounded runs of the other configurations in the headline line")
     args = ap.parse_args()
     if args.cpu_sample is None:
         args.cpu_sample = {"lcurve48": 131072, "chi2k8_48": 131072}.get(args.workload, 16384)
@@ -616,10 +656,11 @@ def main():
     torch.cuda.synchronize()
     replicas.barrier(world)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    k_e2e = max(1, min(args.steps, 5))
+    for _ in range(k_e2e):
         ctx.check(ctx.L.decaes_t2map_t2part(ctx.h, C.byref(mo_c), C.byref(po_c), C.c_void_p(h_img.data_ptr()),
                                             _lib.F32, None, C.byref(hm), C.byref(hp)))
-    e2e_s = replicas.max_over_ranks((time.perf_counter() - t0) / args.steps, world, device="cuda")
+    e2e_s = replicas.max_over_ranks((time.perf_counter() - t0) / k_e2e, world, device="cuda")
     h2d = img.nbytes
     d2h = sum(v.numel() * 4 for v in h_out.values()) + sum(v.numel() * 4 for v in h_parts.values())
     del h_out, h_parts, h_img
@@ -669,7 +710,7 @@ def main():
         "voxels_above_threshold": Vp,
         "voxels_above_threshold_per_s": world * Vp / (ms_per_step * 1e-3),
         "e2e": {"value": world * V / e2e_s, "unit": "voxels/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h, "steps": k_e2e},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
@@ -778,7 +819,55 @@ def main():
                             f"operations (oracle-counted), which the mixed method replaces by fewer"}
     if "roofline" in line:
         line["roofline"]["hbm_view"] = hbm_view(mo, Vp, V, kern_ms)
+    if args.workload == "lcurve48" and args.precision == "mixed" and not args.no_extra and world == 1:
+        line["other_configurations"] = other_configurations(args, D, _lib, ctx, torch)
     print(json.dumps(line), flush=True)
+
+
+def other_configurations(args, D, _lib, ctx, torch):
+    """Bounded runs of the other single-GPU configurations beside the headline:
+    the 56-echo GCV volume's settings on a slab of it (mixed method; FP64 on
+    its first slice for the per-output errors), and a sample of the uneven
+    batch at its stated sizes (one graph replay against one device call per
+    volume)."""
+    out = {}
+    nz = 8
+    wl = WORKLOADS["gcv56"]
+    matrix = (wl["matrix"][0], wl["matrix"][1], nz)
+    V = int(np.prod(matrix))
+    mo, po, mock = workload(matrix, "mixed", "gcv56")
+    img = D.mock_image(mock, seed=args.seed, dtype=np.float32)
+    run = DeviceRun(D, _lib, ctx, torch, mo, po, img, V)
+    ms, _, _ = run.timed(2, 1, 1)
+    Vp = run.stats()["voxels_processed"]
+    head = run.host()
+    del run
+    Vs = matrix[0] * matrix[1]
+    sub = (matrix[0], matrix[1], 1)
+    mo64, po64, _ = workload(sub, "fp64", "gcv56")
+    img_s = np.ascontiguousarray(img.reshape((V, -1), order="F")[:Vs]).reshape((*sub, -1), order="F")
+    run64 = DeviceRun(D, _lib, ctx, torch, mo64, po64, img_s, Vs, f64=True)
+    ms64, _, _ = run64.timed(1, 0, 1)
+    fp64 = run64.host()
+    del run64
+    out["gcv56_slab"] = {
+        "workload": config_dict(matrix, V, "gcv56")["workload"] + f" (the first {nz} of 113 z-slices)",
+        "value": V / (ms * 1e-3), "unit": "voxels/s", "ms_per_step": ms, "steps": 2, "voxels_above_threshold": Vp,
+        "fp64_value": Vs / (ms64 * 1e-3), "fp64_volume": f"{sub[0]}x{sub[1]}x1 (first z-slice), FP64 image and outputs",
+        "speedup_vs_fp64": (V / (ms * 1e-3)) / (Vs / (ms64 * 1e-3)),
+        "errors_vs_fp64": method_errors(*(a[:Vs] for a in head), *fp64),
+    }
+    nvol = 16
+    specs = batch_volume_specs(np.random.default_rng(args.seed + 1), nvol, args.seed + 1000)
+    V_tot, Vp_b, ms_b, ms_seq, V_seq, same = run_batch_groups(ctx, torch, specs, "mixed", nvol, 1, 0, 1)
+    out["batch"] = {
+        "workload": f"{nvol} " + BATCH_DESC.replace("{{", "{").replace("}}", "}") + " (mixed method)",
+        "value": V_tot / (ms_b * 1e-3), "unit": "voxels/s", "ms_per_step": ms_b, "steps": 1, "warmup": 0,
+        "voxels": V_tot, "voxels_above_threshold": Vp_b,
+        "sequential_device_calls": {"value": V_seq / (ms_seq * 1e-3), "ms": ms_seq, "speedup_of_batch": ms_seq / ms_b,
+                                    "same_outputs": bool(same)},
+    }
+    return out
 
 
 def hbm_view(mo, Vp, V, kern_ms):

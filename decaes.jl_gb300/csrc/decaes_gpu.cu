@@ -259,6 +259,7 @@ struct TuneKey {
 };
 struct Tune {
     int wpb = 1;
+    int bps = 0;  // resident blocks per SM of the persistent grid (0: as many as fit)
     double us_per_voxel = 0;
 };
 
@@ -283,6 +284,7 @@ struct decaes_ctx {
     size_t smem_optin = 0;
     std::map<TuneKey, Tune> tune;
     int force_wpb = 0;  // autotuner trials
+    int force_bps = 0;
     int tc_chunks = 0;                 // tensor-core product launches of the last call
     cudaEvent_t tc_ev[2 * kTcEvents];  // their start/end events (the first kTcEvents)
     std::mutex mu;
@@ -489,6 +491,15 @@ int tuned_wpb_or0(decaes_ctx *ctx, const decaes_t2map_opts &o) {
     auto it = ctx->tune.find(k);
     return it == ctx->tune.end() ? 0 : it->second.wpb;
 }
+// Resident blocks per SM for a launch of these options: forced, else
+// autotuned, else 0 (as many as fit).
+int tuned_bps(decaes_ctx *ctx, const decaes_t2map_opts &o) {
+    if (ctx->force_bps) return ctx->force_bps;
+    const bool fixed = !std::isnan(o.SetFlipAngle);
+    TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, is_mixed(o), o.RefConAngle == 180.0, o.legacy != 0};
+    auto it = ctx->tune.find(k);
+    return it == ctx->tune.end() ? 0 : it->second.bps;
+}
 int tuned_wpb(decaes_ctx *ctx, const decaes_t2map_opts &o) {
     const int w = tuned_wpb_or0(ctx, o);
     return w > 0 ? w : 1;
@@ -513,9 +524,10 @@ int most_warps_wpb(decaes_ctx *ctx, Kern kern, long stride, int max_wpb) {
 }
 
 // Persistent grid for a kernel whose warps each need `stride` doubles of
-// shared memory: blocks of wpb warps, as many as fit on every SM at once.
+// shared memory: blocks of wpb warps, as many as fit on every SM at once, or
+// at most bps of them per SM when bps > 0.
 template <class Kern>
-int launch_shape(decaes_ctx *ctx, Kern kern, long stride, int *wpb, int *grid, size_t *smem) {
+int launch_shape(decaes_ctx *ctx, Kern kern, long stride, int *wpb, int *grid, size_t *smem, int bps = 0) {
     for (; *wpb >= 1; *wpb >>= 1) {
         *smem = (size_t)*wpb * stride * sizeof(double);
         if (*smem > ctx->smem_optin) continue;
@@ -523,6 +535,7 @@ int launch_shape(decaes_ctx *ctx, Kern kern, long stride, int *wpb, int *grid, s
         int per_sm = 0;
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * *wpb, *smem));
         if (per_sm >= 1) {
+            if (bps > 0 && bps < per_sm) per_sm = bps;
             *grid = per_sm * ctx->sms;
             return DECAES_OK;
         }
@@ -583,7 +596,7 @@ int run_t2map(decaes_ctx *ctx, const decaes_t2map_opts &o, const decaes_t2part_o
     // the plain method's large workspace: blocks of up to 8 warps can hold a
     // warp per SM more than single-warp blocks (its kernel allows 256 threads)
     if (kern == dk::k_voxels_plain && tuned_wpb_or0(ctx, o) == 0) wpb = most_warps_wpb(ctx, kern, wsm, 8);
-    if (int rc = launch_shape(ctx, kern, wsm, &wpb, &grid, &smem)) return rc;
+    if (int rc = launch_shape(ctx, kern, wsm, &wpb, &grid, &smem, tuned_bps(ctx, o))) return rc;
     void *scr;
     if (int rc = buf(ctx, "scratch", sizeof(double) * (size_t)P.scr_stride * grid * wpb, &scr)) return rc;
     P.scratch = (double *)scr;
@@ -1147,7 +1160,8 @@ int batch_plan(decaes_ctx *ctx, const decaes_volume *vols, int nvol, cudaStream_
         }
         c.kern = dk::batch_kernel(legacy, any_plain, any_mixed);
         c.wpb = tuned_wpb(ctx, bp.vols[c.first].v.mopts);
-        if (int rc = launch_shape(ctx, c.kern, c.smem_stride, &c.wpb, &c.grid, &c.smem)) return rc;
+        if (int rc = launch_shape(ctx, c.kern, c.smem_stride, &c.wpb, &c.grid, &c.smem, tuned_bps(ctx, bp.vols[c.first].v.mopts)))
+            return rc;
         bp.scr_doubles = std::max(bp.scr_doubles, c.scr_stride * c.grid * c.wpb);
     }
     return DECAES_OK;
@@ -1399,32 +1413,61 @@ extern "C" int decaes_autotune(decaes_ctx *ctx, const decaes_t2map_opts *opts, d
     CK(cudaMemcpy(d_img, img.data(), sizeof(float) * img.size(), cudaMemcpyHostToDevice));
     OutMap om;
     if (int rc = out_layout(ctx, o, false, om)) return rc;
+    // Launch shapes tried: warps per block (voxels in flight per block) 1, 2
+    // and 4, each with as many resident blocks per SM as fit and with one and
+    // two fewer (fewer warps sharing an SM's FP64 pipes, L1 and L2 share).
     const int cand[3] = {1, 2, 4};
-    int best_w = 1;
+    int best_w = 1, best_b = 0;
     double best_ms = 1e30;
-    for (int w : cand) {
+    auto trial = [&](int w, int b, float *ms) -> int {
         ctx->force_wpb = w;
+        ctx->force_bps = b;
         float best = 1e30f;
         for (int rep = 0; rep < 2; ++rep) {
             int nl = 0;
-            int rc = run_t2map(ctx, o, nullptr, d_img, DECAES_F32, nullptr, om, ctx->stream, &nl);
-            if (rc) { ctx->force_wpb = 0; return rc; }
+            if (int rc = run_t2map(ctx, o, nullptr, d_img, DECAES_F32, nullptr, om, ctx->stream, &nl)) return rc;
             CK(cudaStreamSynchronize(ctx->stream));
             float t = 0;
             cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]);
             if (rep > 0) best = std::min(best, t);  // first run warms the basis and the caches
         }
-        if (best < best_ms) { best_ms = best; best_w = w; }
+        *ms = best;
+        return DECAES_OK;
+    };
+    for (int w : cand) {
+        float t = 0;
+        int rc = trial(w, 0, &t);
+        if (rc) { ctx->force_wpb = ctx->force_bps = 0; return rc; }
+        if (t < best_ms) { best_ms = t; best_w = w; best_b = 0; }
+        // blocks per SM of the full grid of this block size
+        Basis *B = nullptr;
+        dk::Params P;
+        long wsm = 0;
+        int wpb = w, grid = 0;
+        size_t smem = 0;
+        if ((rc = get_basis(ctx, o, &B)) || (rc = make_params(ctx, o, nullptr, nullptr, B, d_img, DECAES_F32, nullptr, om, P, &wsm))) {
+            ctx->force_wpb = ctx->force_bps = 0;
+            return rc;
+        }
+        auto kern = o.legacy ? dk::k_voxels_legacy : (is_mixed(o) ? dk::k_voxels_mixed : dk::k_voxels_plain);
+        if ((rc = launch_shape(ctx, kern, wsm, &wpb, &grid, &smem))) { ctx->force_wpb = ctx->force_bps = 0; return rc; }
+        if (wpb != w) continue;  // this block size does not fit
+        const int full = grid / ctx->sms;
+        for (int b = full - 1; b >= std::max(1, full - 2); --b) {
+            if ((rc = trial(w, b, &t))) { ctx->force_wpb = ctx->force_bps = 0; return rc; }
+            if (t < best_ms) { best_ms = t; best_w = w; best_b = b; }
+        }
     }
-    ctx->force_wpb = 0;
+    ctx->force_wpb = ctx->force_bps = 0;
     const bool fixed = !std::isnan(o.SetFlipAngle);
     TuneKey k{o.nTE, o.nT2, fixed ? 1 : o.nRefAngles, o.Reg, is_mixed(o), o.RefConAngle == 180.0,
               o.legacy != 0};
     Tune t;
     t.wpb = best_w;
+    t.bps = best_b;
     t.us_per_voxel = best_ms * 1e3 / (double)V;
     ctx->tune[k] = t;
-    if (out) { out->warps_per_block = t.wpb; out->us_per_voxel = t.us_per_voxel; }
+    if (out) { out->warps_per_block = t.wpb; out->us_per_voxel = t.us_per_voxel; out->blocks_per_sm = t.bps; }
     return DECAES_OK;
 }
 
@@ -1713,7 +1756,7 @@ std::vector<Chunk> srv_launch_tick(decaes_server *S) {
         }
         k.kern = dk::batch_kernel(legacy, any_plain, any_mixed);
         k.wpb = tuned_wpb(ctx, ch[k.first].r->mo);
-        ok = launch_shape(ctx, k.kern, k.smem_stride, &k.wpb, &k.grid, &k.smem) == DECAES_OK;
+        ok = launch_shape(ctx, k.kern, k.smem_stride, &k.wpb, &k.grid, &k.smem, tuned_bps(ctx, ch[k.first].r->mo)) == DECAES_OK;
         scr_doubles = std::max(scr_doubles, k.scr_stride * k.grid * k.wpb);
     }
     const size_t need = sizeof(double) * (size_t)scr_doubles;

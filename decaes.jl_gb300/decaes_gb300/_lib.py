@@ -65,7 +65,7 @@ class VolumeC(C.Structure):
 
 
 class TuningC(C.Structure):
-    _fields_ = [("warps_per_block", C.c_int32), ("us_per_voxel", C.c_double)]
+    _fields_ = [("warps_per_block", C.c_int32), ("us_per_voxel", C.c_double), ("blocks_per_sm", C.c_int32)]
 
 
 class ServerOptsC(C.Structure):

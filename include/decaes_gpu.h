@@ -210,13 +210,16 @@ int decaes_batch_run(decaes_batch *batch, void *stream);
 void decaes_batch_destroy(decaes_batch *batch);
 
 /* Autotuner: times the voxel kernel on a synthetic slab of the given shape
- * and method with 1, 2 and 4 warps per block, keeps the fastest for that
- * (nTE, nT2, nRefAngles, Reg, precision, control angle) in the context, and
- * reports it.  Later calls on the context use the tuned shape; batches also
+ * and method for a set of launch shapes -- 1, 2 and 4 warps (voxels in
+ * flight) per block, each with as many resident blocks per SM as fit and with
+ * one and two fewer -- keeps the fastest for that (nTE, nT2, nRefAngles, Reg,
+ * precision, control angle) in the context, and reports it.  Later calls,
+ * batches and server ticks on the context use the tuned shape; batches also
  * use the measured cost to order their queue. */
 typedef struct {
     int32_t warps_per_block;
     double us_per_voxel;       /* device time per above-threshold voxel, whole GPU */
+    int32_t blocks_per_sm;     /* resident blocks per SM (0: as many as fit) */
 } decaes_tuning;
 int decaes_autotune(decaes_ctx *ctx, const decaes_t2map_opts *opts, decaes_tuning *out);
 

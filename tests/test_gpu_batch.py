@@ -128,7 +128,9 @@ def test_autotune_keeps_results(D, ctx):
     before = _single(D, ctx, v)
     t = _lib().TuningC()
     ctx.check(D.load().decaes_autotune(ctx.h, C.byref(v.mo.to_c()), C.byref(t)))
-    assert t.warps_per_block in (1, 2, 4) and t.us_per_voxel > 0
+    assert t.warps_per_block in (1, 2, 4) and t.us_per_voxel > 0 and t.blocks_per_sm >= 0
+    print("tuned:", t.warps_per_block, "warps per block,", t.blocks_per_sm or "all", "blocks per SM,",
+          t.us_per_voxel, "us per voxel")
     v.reset()
     _same(_single(D, ctx, v), before, "tuned")
 
