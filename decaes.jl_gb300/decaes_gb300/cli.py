@@ -5,7 +5,7 @@ reference's `decaes` program (src/main.jl).
         --T2Range 10e-3 2.0 --SPWin 10e-3 25e-3 --MPWin 25e-3 200e-3 --Reg lcurve -o results/
 
 Same arguments and file conventions as the reference (src/main.jl:8-291):
-inputs .mat / .nii / .nii.gz / .par / .rec (one 4-D image each; masks and B1
+inputs .mat / .nii / .nii.gz / .par / .xml / .rec (one 4-D image each; masks and B1
 maps 3-D), `@file` settings files with one argument per line, outputs
 <name>.t2dist.mat ("dist"), <name>.t2maps.mat (the maps dictionary),
 <name>.t2parts.mat (the parts dictionary) and <name>.log in the output folder
@@ -23,6 +23,7 @@ import shutil
 import subprocess
 import sys
 import tempfile
+import threading
 import time
 import warnings
 
@@ -311,6 +312,23 @@ def _try_load_b1(b1file, shape):
 # ---------------------------------------------------------------------------
 # Processing (src/main.jl:272-420)
 # ---------------------------------------------------------------------------
+class ThisThread(logging.Filter):
+    """Passes the records of the thread that made the filter: runs that share
+    the process (a daemon serving several clients at once) keep their logs
+    apart."""
+
+    def __init__(self):
+        super().__init__()
+        self.ident = threading.get_ident()
+
+    def filter(self, record):
+        return record.thread == self.ident
+
+
+_level_lock = threading.Lock()
+_level_users = [0, logging.NOTSET]  # runs logging at INFO, the level to restore after the last
+
+
 @contextlib.contextmanager
 def _tee(logfile, quiet: bool, dry: bool):
     handlers = []
@@ -319,18 +337,26 @@ def _tee(logfile, quiet: bool, dry: bool):
     if not dry and logfile:
         handlers.append(logging.FileHandler(logfile, mode="w"))
     fmt = logging.Formatter("[%(levelname)s] %(message)s")
+    mine = ThisThread()
     for h in handlers:
         h.setFormatter(fmt)
+        h.addFilter(mine)
         log.addHandler(h)
-    old = log.level
-    log.setLevel(logging.INFO)
+    with _level_lock:
+        if _level_users[0] == 0:
+            _level_users[1] = log.level
+        _level_users[0] += 1
+        log.setLevel(logging.INFO)
     try:
         yield
     finally:
         for h in handlers:
             log.removeHandler(h)
             h.close()
-        log.setLevel(old)
+        with _level_lock:
+            _level_users[0] -= 1
+            if _level_users[0] == 0:
+                log.setLevel(_level_users[1])
 
 
 def _timed(msg, fn, *a, **kw):
@@ -341,8 +367,29 @@ def _timed(msg, fn, *a, **kw):
     return r
 
 
-def process_file(info: dict, opts: dict, ctx=None) -> None:
-    from . import api, matfile
+class DirectSolver:
+    """The GPU calls of a run, straight on a context (the command line's own
+    process)."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+
+    def t2map_t2part(self, image, mo, po, b1):
+        from . import api
+        return api.T2mapSEcorr_T2partSEcorr(image, mo, po, b1map=b1, ctx=self.ctx)
+
+    def t2map(self, image, mo, b1):
+        from . import api
+        return api.T2mapSEcorr(image, mo, b1map=b1, ctx=self.ctx)
+
+    def t2part(self, dist, po):
+        from . import api
+        return api.T2partSEcorr(dist, po, ctx=self.ctx)
+
+
+def process_file(info: dict, opts: dict, ctx=None, solver=None) -> None:
+    from . import matfile
+    solver = solver or DirectSolver(ctx)
     t0 = time.time()
     log.info(f"Starting decaes_gb300 (GPU {opts.get('device', 0)}, precision {opts.get('precision', 'fp64')})")
     image = _timed(f"Loading input file: {info['inputfile']}", load_image, info["inputfile"])
@@ -362,10 +409,9 @@ def process_file(info: dict, opts: dict, ctx=None) -> None:
         if opts["T2part"]:
             po = t2part_options(_dist_shape(mo), opts)
             maps, dist, parts = _timed(f"Running T2mapSEcorr and T2partSEcorr on file: {info['inputfile']}",
-                                       api.T2mapSEcorr_T2partSEcorr, image, mo, po, b1map=b1, ctx=ctx)
+                                       solver.t2map_t2part, image, mo, po, b1)
         else:
-            maps, dist = _timed(f"Running T2mapSEcorr on file: {info['inputfile']}", api.T2mapSEcorr, image, mo,
-                                b1map=b1, ctx=ctx)
+            maps, dist = _timed(f"Running T2mapSEcorr on file: {info['inputfile']}", solver.t2map, image, mo, b1)
             parts = None
         if save:
             f = os.path.join(out, stem + ".t2dist.mat")
@@ -377,7 +423,7 @@ def process_file(info: dict, opts: dict, ctx=None) -> None:
     if opts["T2part"]:
         if parts is None:
             po = t2part_options(dist, opts)
-            parts = _timed("Running T2partSEcorr", api.T2partSEcorr, dist, po, ctx=ctx)
+            parts = _timed("Running T2partSEcorr", solver.t2part, dist, po)
         if save:
             f = os.path.join(out, stem + ".t2parts.mat")
             _timed(f"Saving T2 parts maps to file: {f}", matfile.write, f, parts)
@@ -394,12 +440,26 @@ def _dist_shape(mo):
     return _Shape(tuple(mo.MatrixSize) + (mo.nT2,))
 
 
-def run_main(args=None, ctx=None) -> None:
+def _under(cwd, path):
+    return path if path is None or os.path.isabs(path) else os.path.join(cwd, path)
+
+
+def run_main(args=None, ctx=None, cwd=None, solver=None) -> None:
     """main(ARGS): every input file in turn; a failing file is logged and the
-    next one runs (src/main.jl:272-332)."""
+    next one runs (src/main.jl:272-332).  cwd: the directory relative paths
+    (inputs, outputs, masks, B1 maps, @settings files) are taken from, when it
+    is not the process's own (a daemon running a client's command line).
+    solver: the object that makes the GPU calls (DirectSolver on ctx by
+    default)."""
     args = list(sys.argv[1:] if args is None else args)
+    if cwd is not None:
+        args = ["@" + _under(cwd, a[1:]) if a.startswith("@") else a for a in args]
     opts = parse_cli(args)
-    if ctx is None:
+    if cwd is not None:
+        for k in ("input", "output", "mask", "B1map"):
+            if opts.get(k):
+                opts[k] = [_under(cwd, f) for f in opts[k]]
+    if ctx is None and solver is None:
         from ._lib import Context
         ctx = Context(opts.get("device", 0))
     for info in get_file_infos(opts):
@@ -413,7 +473,7 @@ def run_main(args=None, ctx=None) -> None:
         logfile = os.path.join(info["outputfolder"], info["choppedinputfile"] + ".log")
         with _tee(logfile, opts["quiet"], opts["dry"]):
             try:
-                process_file(info, opts, ctx)
+                process_file(info, opts, ctx, solver)
             except Exception as e:
                 log.warning(f"Error during processing of file: {info['inputfile']}")
                 log.warning(f"{type(e).__name__}: {e}")

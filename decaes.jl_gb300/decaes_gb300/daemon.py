@@ -5,14 +5,19 @@ api/decaes_server.jl, which keeps a Julia process warm with DaemonMode so a
 `decaes ...` call skips start-up and compilation; here a call skips Python and
 CUDA start-up and reuses the bases already on the device.
 
-    python -m decaes_gb300.daemon serve [--port P] [--device D]   # start (blocks)
+    python -m decaes_gb300.daemon serve [--port P] [--device D] [--no-batching]
     python -m decaes_gb300.daemon run [--port P] -- <decaes arguments>
     python -m decaes_gb300.daemon ping | kill [--port P]
 
-The server listens on 127.0.0.1 only and runs one command line at a time (in
-the client's working directory, so relative paths mean what they meant to the
-client); the client prints the run's log and exits with its status.
-Protocol: one JSON line each way.
+The server listens on 127.0.0.1 only.  Each client's command line runs in a
+thread of its own, with relative paths taken from the client's working
+directory and its log kept apart from the other runs'.  Their T2map (+
+T2part) work goes to one continuous-batching server on the context
+(decaes_server_*): command lines that arrive while others are on the GPU are
+admitted and solved in the same ticks.  Runs with a B1 map and T2part-only
+runs call the context directly (serialized with the ticks by the library).
+With --no-batching every run calls the context directly.  The client prints
+the run's log and exits with its status.  Protocol: one JSON line each way.
 """
 from __future__ import annotations
 
@@ -29,14 +34,59 @@ import threading
 DEFAULT_PORT = 45867
 
 
-class _Server(socketserver.TCPServer):
-    allow_reuse_address = True
+class BatchingSolver:
+    """The GPU calls of the daemon's runs through one continuous-batching
+    server on the shared context: a run submits its request and waits for
+    it, and requests of concurrent runs share ticks."""
 
-    def __init__(self, port: int, ctx):
+    def __init__(self, ctx):
+        from . import cli
+        from .server import Server
+        self.ctx = ctx
+        self.srv = Server(ctx)
+        self.direct = cli.DirectSolver(ctx)
+
+    def t2map_t2part(self, image, mo, po, b1):
+        if b1 is not None:  # the server takes no B1 map
+            return self.direct.t2map_t2part(image, mo, po, b1)
+        return self.srv.result(self.srv.submit(image, mo, po))
+
+    def t2map(self, image, mo, b1):
+        if b1 is not None:
+            return self.direct.t2map(image, mo, b1)
+        return self.srv.result(self.srv.submit(image, mo, None))
+
+    def t2part(self, dist, po):
+        return self.direct.t2part(dist, po)
+
+    def close(self):
+        self.srv.close()
+
+
+class _Server(socketserver.ThreadingMixIn, socketserver.TCPServer):
+    allow_reuse_address = True
+    daemon_threads = True
+
+    def __init__(self, port: int, ctx, batching: bool = True):
         super().__init__(("127.0.0.1", port), _Handler)
         self.ctx = ctx
         self.runs = 0
         self.lock = threading.Lock()
+        self.batching = batching
+        self._solver = None
+
+    def solver(self):
+        from . import cli
+        with self.lock:
+            if self._solver is None:
+                self._solver = BatchingSolver(self.ctx) if self.batching else cli.DirectSolver(self.ctx)
+            return self._solver
+
+    def server_close(self):
+        super().server_close()
+        if self._solver is not None and hasattr(self._solver, "close"):
+            self._solver.close()
+            self._solver = None
 
 
 class _Handler(socketserver.StreamRequestHandler):
@@ -56,21 +106,20 @@ class _Handler(socketserver.StreamRequestHandler):
         buf = io.StringIO()
         handler = logging.StreamHandler(buf)
         handler.setFormatter(logging.Formatter("[%(levelname)s] %(message)s"))
+        handler.addFilter(cli.ThisThread())  # this run's records only
         status = 0
-        with self.server.lock:
-            old = os.getcwd()
-            cli.log.addHandler(handler)
-            try:
-                os.chdir(req.get("cwd") or old)
-                cli.run_main(list(req.get("args", [])), ctx=self.server.ctx)
-            except SystemExit as e:  # argparse: --help, usage errors
-                status = e.code if isinstance(e.code, int) else 1
-            except Exception as e:
-                buf.write(f"[ERROR] {type(e).__name__}: {e}\n")
-                status = 1
-            finally:
-                cli.log.removeHandler(handler)
-                os.chdir(old)
+        cli.log.addHandler(handler)
+        try:
+            cli.run_main(list(req.get("args", [])), ctx=self.server.ctx, cwd=req.get("cwd") or os.getcwd(),
+                         solver=self.server.solver())
+        except SystemExit as e:  # argparse: --help, usage errors
+            status = e.code if isinstance(e.code, int) else 1
+        except Exception as e:
+            buf.write(f"[ERROR] {type(e).__name__}: {e}\n")
+            status = 1
+        finally:
+            cli.log.removeHandler(handler)
+            with self.server.lock:
                 self.server.runs += 1
         return self._reply({"status": status, "log": buf.getvalue()})
 
@@ -79,13 +128,14 @@ class _Handler(socketserver.StreamRequestHandler):
         self.wfile.flush()
 
 
-def make_server(port: int = DEFAULT_PORT, ctx=None, device: int = 0) -> _Server:
+def make_server(port: int = DEFAULT_PORT, ctx=None, device: int = 0, batching: bool = True) -> _Server:
     """The server object (call serve_forever() on it); ctx defaults to a new
-    context on `device`."""
+    context on `device`.  batching: the runs' GPU work goes through one
+    continuous-batching server (else straight to the context)."""
     if ctx is None:
         from ._lib import Context
         ctx = Context(device)
-    return _Server(port, ctx)
+    return _Server(port, ctx, batching)
 
 
 def request(obj: dict, port: int = DEFAULT_PORT, timeout: float | None = None) -> dict:
@@ -115,9 +165,10 @@ def main(argv=None) -> int:
     ap.add_argument("command", choices=("serve", "run", "ping", "kill"))
     ap.add_argument("--port", type=int, default=DEFAULT_PORT)
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--no-batching", action="store_true", help="serve: run each command line straight on the context")
     a, rest = ap.parse_known_args(argv)
     if a.command == "serve":
-        srv = make_server(a.port, device=a.device)
+        srv = make_server(a.port, device=a.device, batching=not a.no_batching)
         print(f"decaes_gb300 daemon on 127.0.0.1:{a.port} (GPU {a.device})", flush=True)
         try:
             srv.serve_forever()

@@ -5,7 +5,8 @@
 #   --python PATH   Python interpreter (default: python3)
 #   --server        forward the command line to a running warm daemon
 #                   (python -m decaes_gb300.daemon serve) instead of starting
-#                   a new process
+#                   a new process; command lines forwarded at the same time
+#                   run concurrently and share the daemon's batching server
 #   --port P        the daemon's port (with --server)
 set -e
 here="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"

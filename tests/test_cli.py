@@ -117,8 +117,49 @@ def test_parrec(D, tmp_path, cli):
         assert img.shape == (nx, ny, 2, 3)
         for sl, ec, pv in images:
             np.testing.assert_allclose(img[:, :, sl - 1, ec - 1], (pv * rs + ri) / (rs * ss), rtol=1e-15)
-    with pytest.raises(ValueError, match="XML"):
-        cli.load_image(str(tmp_path / "scan.xml"))
+
+
+def _write_xmlrec(base, images, nx, ny, ri, rs, ss):
+    """The same images with a Philips XML header (one <Image_Info> per stored
+    image: a <Key> with Slice/Echo/Dynamic/Phase/BValue/Grad Orient/Label
+    Type/Type/Sequence/Index, then the image's attributes)."""
+    def attr(name, typ, val):
+        return f'<Attribute Name="{name}" Type="{typ}">{val}</Attribute>'
+    order = list(range(len(images)))[::-1]
+    rec = bytearray()
+    for i in order:
+        rec += np.asarray(images[i][2], dtype="<i2").tobytes(order="F")
+    infos = []
+    for i, (sl, ec, _) in enumerate(images):
+        key = "".join([attr("Slice", "Int32", sl), attr("Echo", "Int32", ec), attr("Dynamic", "Int32", 1),
+                       attr("Phase", "Int32", 1), attr("BValue", "Int32", 1), attr("Grad Orient", "Int32", 1),
+                       attr("Label Type", "Enumeration", "-"), attr("Type", "Enumeration", "M"),
+                       attr("Sequence", "Enumeration", "SE"), attr("Index", "Int32", order.index(i))])
+        rest = "".join([attr("Pixel Size", "UInt16", 16), attr("Resolution X", "UInt16", nx),
+                        attr("Resolution Y", "UInt16", ny), attr("Rescale Intercept", "Double", ri),
+                        attr("Rescale Slope", "Double", rs), attr("Scale Slope", "Float", ss),
+                        attr("Echo Time", "Float", 10.0 * ec)])
+        infos.append(f"<Image_Info><Key>{key}</Key>{rest}</Image_Info>")
+    xml = ('<?xml version="1.0" encoding="UTF-8"?><PRIDE_V5><Series_Info>' + attr("Max No Slices", "UInt16", 2) +
+           "</Series_Info><Image_Array>" + "".join(infos) + "</Image_Array></PRIDE_V5>")
+    (base.parent / (base.name + ".XML")).write_text(xml)
+    (base.parent / (base.name + ".REC")).write_bytes(bytes(rec))
+
+
+def test_xmlrec(D, tmp_path, cli):
+    """An XML/REC pair reads as the same image as the PAR/REC pair of the same
+    data (ParXRec.jl's XML form; no scanner file is available here, so the
+    header follows the published layout written by _write_xmlrec)."""
+    nx, ny, ri, rs, ss = 4, 5, -3.0, 2.5, 0.125
+    rng = np.random.default_rng(5)
+    images = [(sl, ec, rng.integers(0, 4000, size=(nx, ny))) for sl in (1, 2) for ec in (1, 2, 3)]
+    (tmp_path / "p").mkdir()
+    (tmp_path / "x").mkdir()
+    _write_parrec(tmp_path / "p" / "scan", images, nx, ny, ri, rs, ss)
+    _write_xmlrec(tmp_path / "x" / "scan", images, nx, ny, ri, rs, ss)
+    want = cli.load_image(str(tmp_path / "p" / "scan.PAR"))
+    for name in ("scan.XML", "scan.REC"):
+        np.testing.assert_array_equal(cli.load_image(str(tmp_path / "x" / name)), want)
 
 
 def test_ensure_ndims(D, cli, caplog):

@@ -77,3 +77,52 @@ def test_daemon_on_gpu(D, ctx, tmp_path, monkeypatch):
     maps, dist = D.T2mapSEcorr(np.asfortranarray(img, dtype=np.float64), mo, ctx=ctx)
     np.testing.assert_array_equal(io.loadmat(str(tmp_path / "r1" / "a.t2dist.mat"))["dist"], dist)
     assert (tmp_path / "r2" / "a.t2maps.mat").exists()
+
+
+def test_daemon_clients_share_the_batching_server(D, ctx, tmp_path):
+    """Four clients at once: their command lines run concurrently in the
+    daemon and their T2map+T2part work goes to one continuous-batching server
+    (decaes_server_*); every client's outputs equal the direct API call's."""
+    import socket
+    import threading
+    io = pytest.importorskip("scipy.io")
+    from decaes_gb300 import daemon, nifti
+    X = (24, 20, 3)
+    imgs = [D.mock_image(D.MockImageOptions(MatrixSize=X, nTE=32, TE=10e-3), seed=40 + i) for i in range(4)]
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    srv = daemon.make_server(port, ctx=ctx)
+    th = threading.Thread(target=srv.serve_forever, daemon=True)
+    th.start()
+    args = ["img.nii", "--T2map", "--T2part", "--TE", "10e-3", "--nT2", "40", "--T2Range", "10e-3", "2.0", "--Reg",
+            "chi2", "--RegParams", "1.02", "--SPWin", "10e-3", "25e-3", "--MPWin", "25e-3", "200e-3", "-o", "out",
+            "--quiet"]
+    status = {}
+
+    def client(i):
+        d = tmp_path / f"c{i}"
+        d.mkdir()
+        nifti.write(str(d / "img.nii"), imgs[i])
+        status[i] = daemon.request({"cmd": "run", "cwd": str(d), "args": args}, port, timeout=300)
+
+    try:
+        ts = [threading.Thread(target=client, args=(i,)) for i in range(4)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join(timeout=300)
+        sv = srv.solver().srv.stats()
+    finally:
+        srv.shutdown()
+        srv.server_close()
+    assert sv["completed"] == 4 and sv["failed"] == 0
+    mo = D.T2mapOptions(MatrixSize=X, nTE=32, TE=10e-3, nT2=40, T2Range=(10e-3, 2.0), Reg="chi2", Chi2Factor=1.02)
+    po = D.T2partOptions.from_t2map(mo, SPWin=(10e-3, 25e-3), MPWin=(25e-3, 200e-3))
+    for i in range(4):
+        assert status[i]["status"] == 0, status[i]["log"]
+        maps, dist, parts = D.T2mapSEcorr_T2partSEcorr(np.asfortranarray(imgs[i], dtype=np.float64), mo, po, ctx=ctx)
+        out = tmp_path / f"c{i}" / "out"
+        np.testing.assert_array_equal(io.loadmat(str(out / "img.t2dist.mat"))["dist"], dist)
+        np.testing.assert_array_equal(io.loadmat(str(out / "img.t2parts.mat"))["sfr"], parts["sfr"])

@@ -34,7 +34,7 @@ def test_daemon(D, tmp_path, monkeypatch, capsys):
     st = _Stubs(monkeypatch)
     img, mask = _inputs(tmp_path)
     port = _free_port()
-    srv = daemon.make_server(port, ctx=object())
+    srv = daemon.make_server(port, ctx=object(), batching=False)
     th = threading.Thread(target=srv.serve_forever, daemon=True)
     th.start()
     try:
@@ -54,4 +54,50 @@ def test_daemon(D, tmp_path, monkeypatch, capsys):
     finally:
         if th.is_alive():
             srv.shutdown()
+        srv.server_close()
+
+
+def test_daemon_runs_clients_concurrently(D, tmp_path, monkeypatch):
+    """Two clients' command lines run at the same time in the daemon (a
+    solver that lets neither finish until both have reached the GPU call),
+    each in its own working directory and with its own log."""
+    from decaes_gb300 import daemon
+    from test_cli import BASE, _inputs, _Stubs
+    meet = threading.Barrier(2, timeout=30)
+
+    class MeetingSolver:
+        def t2map(self, image, mo, b1):
+            meet.wait()  # raises BrokenBarrierError after 30 s if the runs were serialized
+            return _Stubs.maps(mo), _Stubs.dist(mo)
+
+    port = _free_port()
+    srv = daemon.make_server(port, ctx=object(), batching=False)
+    monkeypatch.setattr(srv, "solver", lambda: MeetingSolver())
+    th = threading.Thread(target=srv.serve_forever, daemon=True)
+    th.start()
+    dirs = [tmp_path / "a", tmp_path / "b"]
+    results = {}
+
+    def client(d):
+        d.mkdir()
+        _inputs(d)
+        results[d.name] = daemon.request({"cmd": "run", "cwd": str(d),
+                                          "args": ["img.nii.gz", "-o", "out"] + BASE}, port, timeout=60)
+
+    try:
+        ts = [threading.Thread(target=client, args=(d,)) for d in dirs]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join(timeout=90)
+        for d in dirs:
+            r = results[d.name]
+            assert r["status"] == 0, r["log"]
+            assert (d / "out" / "img.t2maps.mat").exists()
+            # each log names its own input file only
+            assert str(d / "img.nii.gz") in r["log"]
+            other = dirs[1 - dirs.index(d)]
+            assert str(other / "img.nii.gz") not in r["log"]
+    finally:
+        srv.shutdown()
         srv.server_close()
