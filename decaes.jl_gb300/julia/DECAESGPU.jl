@@ -95,6 +95,11 @@ ptr(x) = x === nothing ? C_NULL : Ptr{Cvoid}(pointer(x))
     T2mapSEcorr(image::Array{T,4}, opts::T2mapOptions{T}; B1map = nothing, precision = :fp64)
 
 GPU counterpart of `DECAES.T2mapSEcorr`: same options, same outputs.
+A Float32 `image` is widened to Float64 on the GPU and computed in Float64
+(`precision = :fp64`, the default) or with the mixed method (`:mixed`,
+`:mixed_tc`), and the results are returned as Float32 -- where DECAES.jl's own
+`T2mapSEcorr(::Array{Float32,4})` computes in Float32.  Pass Float64 for
+results equal to DECAES.jl's Float64 path.
 """
 function T2mapSEcorr(image::Array{T, 4}, opts::T2mapOptions{T}; B1map = nothing, precision::Symbol = :fp64) where {T <: Union{Float32, Float64}}
     @assert size(image) == (opts.MatrixSize..., opts.nTE)

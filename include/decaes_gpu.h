@@ -146,7 +146,10 @@ int decaes_t2part_check_options(const decaes_t2part_opts *opts, char *msg, size_
  * Host buffers.  b1map (V values of the call dtype) replaces the flip-angle
  * search by the given angles, as load_B1map! does (src/T2mapSEcorr.jl:56-61).
  * The plain method computes in FP64 whatever the dtype (FP32 input is widened
- * on the device, as the reference CLI does in src/main.jl:612-617). */
+ * on the device, as the reference CLI does in src/main.jl:612-617); the Julia
+ * API of the reference computes a Float32 image in Float32 (src/types.jl:19),
+ * so for Float32 input the results here are the FP64 results rounded to
+ * Float32, not the reference's single-precision ones. */
 int decaes_t2map(decaes_ctx *ctx, const decaes_t2map_opts *opts, const void *image, int dtype,
                  const void *b1map, decaes_t2map_out *out);
 
