@@ -209,25 +209,29 @@ static __device__ __noinline__ bool gram_refactor(GramWS g, int k, double mu2) {
     const int p0 = r0 < k ? g.P[r0] : 0, p1 = r1 < k ? g.P[r1] : 0;
     double *L0 = g.L + tri(r0 - 1), *L1 = g.L + tri(r1 - 1);
     double *cu = g.xp;  // unscaled pivot column of the current step
-    // strictly lower triangle and diagonal of H_PP, one row per lane
+    // strictly lower triangle and diagonal of H_PP, one row per lane, and each
+    // row's pivot threshold tol * H_rr
+    double th0 = 0.0, th1 = 0.0;
     if (r0 < k) {
         #pragma unroll 1
         for (int c = 0; c < r0; ++c) L0[c] = g.G[gidx(p0, g.P[c])];
-        g.dd[r0] = g.G[tri(p0) + p0] + mu2;
+        const double h = g.G[tri(p0) + p0] + mu2;
+        g.dd[r0] = h;
+        th0 = kGramDepTol * h;
     }
     if (r1 < k) {
         #pragma unroll 1
         for (int c = 0; c < r1; ++c) L1[c] = g.G[gidx(p1, g.P[c])];
-        g.dd[r1] = g.G[tri(p1) + p1] + mu2;
+        const double h = g.G[tri(p1) + p1] + mu2;
+        g.dd[r1] = h;
+        th1 = kGramDepTol * h;
     }
     double v0 = r0 < k ? g.f[p0] : 0.0, v1 = r1 < k ? g.f[p1] : 0.0;
     __syncwarp();
     #pragma unroll 1
     for (int j = 0; j < k; ++j) {
         const double d = g.dd[j];
-        const int pj = g.P[j];
-        const double h = g.G[tri(pj) + pj] + mu2;
-        if (!(d > kGramDepTol * h)) return false;
+        if (!gt_nonneg_bits(d, lane_pick(th0, th1, j))) return false;  // d > tol * H_jj
         const double rd = fast_rcp(d);
         const double yj = lane_pick(v0, v1, j);
         if (r0 > j && r0 < k) {
@@ -284,12 +288,13 @@ static __device__ __noinline__ bool gram_append(GramWS g, int k, int t, double m
     double w0 = 0.0, w1 = 0.0, pl = 0.0, py = 0.0;
     if (r0 < k) { w0 = v0 * g.dinv[r0]; pl = fma(v0, w0, pl); py = fma(w0, g.y[r0], py); }
     if (r1 < k) { w1 = v1 * g.dinv[r1]; pl = fma(v1, w1, pl); py = fma(w1, g.y[r1], py); }
-    const double ll = wsum(pl), ly = wsum(py);
+    double ll, ly;
+    wsum2(pl, py, ll, ly);
     const double htt = g.G[tri(t) + t] + mu2;
     const double delta = htt - ll;
-    if (!(delta > kGramDepTol * htt)) return false;
+    if (!gt_nonneg_bits(delta, kGramDepTol * htt)) return false;
     const double yt = g.f[t] - ly;
-    if (!(yt > 0)) return false;
+    if (!pos_bits(yt)) return false;
     double *Lk = g.L + tri(k - 1);
     if (r0 < k) Lk[r0] = w0;
     if (r1 < k) Lk[r1] = w1;
@@ -498,7 +503,7 @@ static __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double 
             }
             const double2 zz = gram_back(g, k);
             const double z0 = zz.x, z1 = zz.y;
-            const bool keep0 = r0 < k && z0 > 0, keep1 = r1 < k && z1 > 0;
+            const bool keep0 = r0 < k && pos_bits(z0), keep1 = r1 < k && pos_bits(z1);
             const unsigned m0 = __ballot_sync(FULL, keep0), m1 = __ballot_sync(FULL, keep1);
             const int kk = __popc(m0) + __popc(m1);
             if (kk == k) {
@@ -559,7 +564,7 @@ static __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double 
         for (int j = lane; j < n; j += 32) {
             if (g.pos[j] >= 0 || ((rejected >> j) & 1ull)) continue;
             const double wj = wv[j];
-            if (!(wj > 0)) continue;
+            if (!pos_bits(wj)) continue;
             const long long key = okey(wj);
             if (key > best) { best = key; bj = j; }
         }
@@ -576,7 +581,7 @@ static __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double 
         for (;;) {
             const double2 zz = gram_back(g, k);
             const double z0 = zz.x, z1 = zz.y;
-            const bool pos0 = !(r0 < k) || z0 > 0, pos1 = !(r1 < k) || z1 > 0;
+            const bool pos0 = !(r0 < k) || pos_bits(z0), pos1 = !(r1 < k) || pos_bits(z1);
             if (__all_sync(FULL, pos0 && pos1)) {
                 if (r0 < k) x[g.P[r0]] = z0;
                 if (r1 < k) x[g.P[r1]] = z1;
@@ -587,10 +592,11 @@ static __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double 
             // alpha = min over z_r <= 0 of x_r / (x_r - z_r)
             double a0 = CUDART_INF, a1 = CUDART_INF;
             const double x0 = r0 < k ? x[g.P[r0]] : 0.0, x1 = r1 < k ? x[g.P[r1]] : 0.0;
-            if (r0 < k && !(z0 > 0)) a0 = (x0 - z0 > 0) ? x0 * fast_rcp(x0 - z0) : 0.0;
-            if (r1 < k && !(z1 > 0)) a1 = (x1 - z1 > 0) ? x1 * fast_rcp(x1 - z1) : 0.0;
-            long long ka = okey(a0 <= a1 ? a0 : a1);
-            int ia = a0 <= a1 ? r0 : r1;
+            if (r0 < k && !pos_bits(z0)) { const double dz = x0 - z0; a0 = pos_bits(dz) ? x0 * fast_rcp(dz) : 0.0; }
+            if (r1 < k && !pos_bits(z1)) { const double dz = x1 - z1; a1 = pos_bits(dz) ? x1 * fast_rcp(dz) : 0.0; }
+            const long long ka0 = okey(a0), ka1 = okey(a1);  // a0, a1 are not NaN: min without the FP64 pipe
+            long long ka = ka0 <= ka1 ? ka0 : ka1;
+            int ia = ka0 <= ka1 ? r0 : r1;
             warp_keymin(ka, ia);
             const double alpha = lane_pick(a0, a1, ia);
             double nx0 = x0, nx1 = x1;
@@ -598,7 +604,7 @@ static __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double 
             if (r1 < k) nx1 = fma(alpha, z1 - x1, x1);
             if (r0 == ia) nx0 = 0.0;
             if (r1 == ia) nx1 = 0.0;
-            const bool keep0 = r0 < k && nx0 > 0, keep1 = r1 < k && nx1 > 0;
+            const bool keep0 = r0 < k && pos_bits(nx0), keep1 = r1 < k && pos_bits(nx1);
             const unsigned m0 = __ballot_sync(FULL, keep0), m1 = __ballot_sync(FULL, keep1);
             const int p0 = r0 < k ? g.P[r0] : -1, p1 = r1 < k ? g.P[r1] : -1;
             __syncwarp();

@@ -56,6 +56,29 @@ __device__ __forceinline__ long long okey(double d) {
 __device__ __forceinline__ bool isnan_bits(double d) {
     return (__double_as_longlong(d) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
 }
+// d > 0 on the integer pipes (false for zeros and NaN).
+__device__ __forceinline__ bool pos_bits(double d) {
+    const long long b = __double_as_longlong(d);
+    return b > 0 && b <= 0x7ff0000000000000LL;
+}
+// d > t for a threshold t >= 0 or NaN, on the integer pipes: positive doubles
+// order like their bit patterns; negative d and NaN d give false, and so does
+// every d against a NaN threshold, as the FP64 comparison does.
+__device__ __forceinline__ bool gt_nonneg_bits(double d, double t) {
+    const long long b = __double_as_longlong(d);
+    return b > __double_as_longlong(t) && b <= 0x7ff0000000000000LL && !isnan_bits(t);
+}
+// wsum of two values at once: the first butterfly step exchanges a and b
+// between the warp halves, so both sums take five additions instead of ten;
+// each sum is added in wsum's order, so the results are wsum's bit for bit.
+__device__ __forceinline__ void wsum2(double a, double b, double &sa, double &sb) {
+    const bool hi = (threadIdx.x & 16) != 0;
+    double v = __dadd_rn(hi ? b : a, __shfl_xor_sync(FULL, hi ? a : b, 16));
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(FULL, v, o));
+    sa = __shfl_sync(FULL, v, 0);
+    sb = __shfl_sync(FULL, v, 16);
+}
 
 // Per-warp views of the NNLS workspace (shared memory).
 struct NnlsWS {

@@ -931,17 +931,23 @@ static __device__ void fa_update(Search &S, int I) {
     for (int i0 = 0; i0 < (kLegacyKernel && P.legacy ? 0 : m); i0 += 32) {  // legacy: loss! only, src/splines.jl:1043-1046
         int i = i0 + lane;
         double ax = 0, dax = 0;
-        if (i < m) {
-            #pragma unroll 1
-            for (int j = 0; j < n; ++j) {
-                double xj = w.s.x[j];
-                if (xj > 0) {
+        // the columns with x_j > 0 in increasing order, from one ballot per 32
+        // columns instead of a comparison per column
+        #pragma unroll 1
+        for (int j0 = 0; j0 < n; j0 += 32) {
+            unsigned msk = __ballot_sync(FULL, j0 + lane < n && pos_bits(w.s.x[j0 + lane]));
+            if (i < m) {
+                #pragma unroll 1
+                while (msk) {
+                    const int j = j0 + __ffs(msk) - 1;
+                    msk &= msk - 1;
+                    const double xj = w.s.x[j];
                     ax = fma(xj, __ldg(A + i + (long)j * m), ax);
                     dax = fma(xj, __ldg(dA + i + (long)j * m), dax);
                 }
             }
-            part = fma(dax, ax - w.data[i], part);
         }
+        if (i < m) part = fma(dax, ax - w.data[i], part);
     }
     double dt = wsum(part);
     if (lane == 0) {
