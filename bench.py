@@ -661,6 +661,7 @@ def main():
         ctx.check(ctx.L.decaes_t2map_t2part(ctx.h, C.byref(mo_c), C.byref(po_c), C.c_void_p(h_img.data_ptr()),
                                             _lib.F32, None, C.byref(hm), C.byref(hp)))
     e2e_s = replicas.max_over_ranks((time.perf_counter() - t0) / k_e2e, world, device="cuda")
+    e2e_st = ctx.stats()  # the last call's own event timings (copies and the whole call on its stream)
     h2d = img.nbytes
     d2h = sum(v.numel() * 4 for v in h_out.values()) + sum(v.numel() * 4 for v in h_parts.values())
     del h_out, h_parts, h_img
@@ -710,7 +711,8 @@ def main():
         "voxels_above_threshold": Vp,
         "voxels_above_threshold_per_s": world * Vp / (ms_per_step * 1e-3),
         "e2e": {"value": world * V / e2e_s, "unit": "voxels/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "steps": k_e2e},
+                "d2h_bytes_per_step": d2h, "steps": k_e2e,
+                "last_call_ms": {k: round(e2e_st[k], 2) for k in ("ms_h2d", "ms_solve", "ms_d2h", "ms_total")}},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
