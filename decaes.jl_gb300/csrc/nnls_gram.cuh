@@ -84,6 +84,16 @@ __device__ __forceinline__ double fast_rcp(double d) {
     const double e = fma(-d, r, 1.0);
     return fma(r, fma(e, e, e), r);
 }
+// 1/d to ~2^-40 relative: the same seed refined by one quadratic Newton step
+// r(1 + e) (error e^2).  For the pivots of the factorization, whose scaled
+// columns and reciprocals carry that error into the solution at ~1e-12
+// relative (times the passive block's conditioning), below what the mixed
+// method's FP32 basis already moves it; one FP64 instruction fewer per pivot.
+__device__ __forceinline__ double pivot_rcp(double d) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+    return fma(r, fma(-d, r, 1.0), r);
+}
 
 __device__ __forceinline__ double lane_pick(double v0, double v1, int i) {
     // value held for row i (rows i < 32 in v0, rows >= 32 in v1) broadcast from its lane
@@ -200,8 +210,8 @@ static __device__ __noinline__ void gram_load(GramWS &g, const double *Gg, int n
 // LDL' factorization of H_PP = G_PP + mu2 I from scratch (right-looking),
 // with y = L^{-1} f_P carried along as an extra column.  Per pivot: one
 // reciprocal, the column scaled by the lanes of its rows, and the trailing
-// update spread over lanes by (row, column) pair, so a step costs ~(k-j)^2/64
-// FMA instructions instead of k-j.  Returns false when a pivot is not
+// update -- diagonal included -- spread over lanes by (row, column) pair, so a
+// step costs ~(k-j)^2/64 FMA instructions instead of k-j.  Returns false when a pivot is not
 // positive relative to its diagonal (numerically dependent set).
 static __device__ __noinline__ bool gram_refactor(GramWS g, int k, double mu2) {
     const int lane = threadIdx.x & 31;
@@ -232,34 +242,33 @@ static __device__ __noinline__ bool gram_refactor(GramWS g, int k, double mu2) {
     for (int j = 0; j < k; ++j) {
         const double d = g.dd[j];
         if (!gt_nonneg_bits(d, lane_pick(th0, th1, j))) return false;  // d > tol * H_jj
-        const double rd = fast_rcp(d);
+        const double rd = pivot_rcp(d);
         const double yj = lane_pick(v0, v1, j);
         if (r0 > j && r0 < k) {
             const double c0 = L0[j], l0 = c0 * rd;
             L0[j] = l0;
             cu[r0] = c0;
-            g.dd[r0] = fma(-c0, l0, g.dd[r0]);
             v0 = fma(-l0, yj, v0);
         }
         if (r1 > j && r1 < k) {
             const double c1 = L1[j], l1 = c1 * rd;
             L1[j] = l1;
             cu[r1] = c1;
-            g.dd[r1] = fma(-c1, l1, g.dd[r1]);
             v1 = fma(-l1, yj, v1);
         }
         if (lane == 0) g.dinv[j] = rd;
         __syncwarp();
-        // trailing strictly-lower entries (r, c), j < c < r < k, one per lane
-        const int t = k - 1 - j, npair = t * (t - 1) / 2;
+        // trailing lower entries (r, c), j < c <= r < k, one per lane: the
+        // strictly-lower ones in L and the running diagonal (c == r) in dd
+        const int t = k - 1 - j, npair = t * (t + 1) / 2;
         #pragma unroll 1
         for (int q = lane; q < npair; q += 32) {
-            int a = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)q)) * 0.5f);
-            while (a * (a - 1) / 2 > q) --a;
-            while ((a + 1) * a / 2 <= q) ++a;
-            const int r = j + 1 + a, c = j + 1 + (q - a * (a - 1) / 2);
-            double *Lr = g.L + tri(r - 1);
-            Lr[c] = fma(-cu[r], g.L[tri(c - 1) + j], Lr[c]);
+            int a = (int)((sqrtf(8.0f * (float)q + 1.0f) - 1.0f) * 0.5f);
+            while (a * (a + 1) / 2 > q) --a;
+            while ((a + 1) * (a + 2) / 2 <= q) ++a;
+            const int r = j + 1 + a, c = j + 1 + (q - a * (a + 1) / 2);
+            double *e = c == r ? g.dd + r : g.L + tri(r - 1) + c;
+            *e = fma(-cu[r], g.L[tri(c - 1) + j], *e);
         }
         __syncwarp();
     }
@@ -300,7 +309,7 @@ static __device__ __noinline__ bool gram_append(GramWS g, int k, int t, double m
     if (r1 < k) Lk[r1] = w1;
     if (lane == 0) {
         g.dd[k] = delta;
-        g.dinv[k] = fast_rcp(delta);
+        g.dinv[k] = pivot_rcp(delta);
         g.y[k] = yt;
         g.P[k] = t;
         g.pos[t] = k;
@@ -538,19 +547,27 @@ static __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double 
         if (dual_stale) {
             #pragma unroll 1
             for (int r = lane; r < k; r += 32) g.xp[r] = x[g.P[r]];
+            // the free columns in column order, compacted into idx (free until
+            // the outputs), so that up to 32 of them take one round of lanes
+            // (only free columns' duals are read)
+            const bool fr0 = r0 < n && g.pos[r0] < 0, fr1 = r1 < n && g.pos[r1] < 0;
+            const unsigned b0 = __ballot_sync(FULL, fr0), b1 = __ballot_sync(FULL, fr1);
+            const unsigned below = (1u << lane) - 1u;
+            if (fr0) idx[__popc(b0 & below)] = r0;
+            if (fr1) idx[__popc(b0) + __popc(b1 & below)] = r1;
+            const int nf = __popc(b0) + __popc(b1);
             __syncwarp();
             #pragma unroll 1
-            for (int j = lane; j < n; j += 32) {
+            for (int i = lane; i < nf; i += 32) {
+                const int j = idx[i];
                 double s = g.f[j], s2 = 0.0;
-                if (g.pos[j] < 0) {
-                    int r = 0;
-                    #pragma unroll 1
-                    for (; r + 1 < k; r += 2) {
-                        s = fma(-g.G[gidx(j, g.P[r])], g.xp[r], s);
-                        s2 = fma(-g.G[gidx(j, g.P[r + 1])], g.xp[r + 1], s2);
-                    }
-                    if (r < k) s = fma(-g.G[gidx(j, g.P[r])], g.xp[r], s);
+                int r = 0;
+                #pragma unroll 1
+                for (; r + 1 < k; r += 2) {
+                    s = fma(-g.G[gidx(j, g.P[r])], g.xp[r], s);
+                    s2 = fma(-g.G[gidx(j, g.P[r + 1])], g.xp[r + 1], s2);
                 }
+                if (r < k) s = fma(-g.G[gidx(j, g.P[r])], g.xp[r], s);
                 wv[j] = s + s2;
             }
             __syncwarp();
