@@ -667,8 +667,7 @@ static __device__ __noinline__ NnlsResult gram_nnls(GramWS g, double *x, double 
         fx = fma(g.f[g.P[r]], xr, fx);
         xx = fma(xr, xr, xx);
     }
-    fx = wsum(fx);
-    xx = wsum(xx);
+    wsum2(fx, xx, fx, xx);  // the same pairings as wsum, both sums in one butterfly
     const double res = fmax(g.bb - fx - mu2 * xx, 0.0);
     NnlsResult out;
     out.nsetp = k;

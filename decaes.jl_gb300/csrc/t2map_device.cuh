@@ -144,9 +144,12 @@ static __device__ TikhState tikh_solve(Warp &w, double mu) {
     note(w, t.r);
     return t;
 }
-static __device__ double tikh_res2(Warp &w, const TikhState &t) {
-    double ssq = warp_seminorm_sq(w.s, t.r.nsetp);
+// ||A x - b||^2 of a Tikhonov solution from its padded residual and ||x||^2.
+static __device__ double tikh_res2_ssq(const TikhState &t, double ssq) {
     return jmax(__dsub_rn(__dmul_rn(t.r.rnorm, t.r.rnorm), __dmul_rn(__dmul_rn(t.mu, t.mu), ssq)), 0.0);
+}
+static __device__ double tikh_res2(Warp &w, const TikhState &t) {
+    return tikh_res2_ssq(t, warp_seminorm_sq(w.s, t.r.nsetp));
 }
 static __device__ void save_x(Warp &w) {
     #pragma unroll 1
@@ -458,8 +461,8 @@ static __device__ DK_OUTLINE void lc_eval(LCurve &L, double x, double &P0, doubl
     Warp &w = *L.w;
     TikhState t = tikh_solve(w, pm_exp(x));
     sol_store(w, x);
-    double res2 = tikh_res2(w, t);
     double ssq = warp_seminorm_sq(w.s, t.r.nsetp);
+    double res2 = tikh_res2_ssq(t, ssq);
     P0 = pm_log(res2);
     P1 = pm_log(ssq);
     if (L.flen < kCacheCap) {
