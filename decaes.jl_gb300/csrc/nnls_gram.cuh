@@ -84,16 +84,6 @@ __device__ __forceinline__ double fast_rcp(double d) {
     const double e = fma(-d, r, 1.0);
     return fma(r, fma(e, e, e), r);
 }
-// 1/d to ~2^-40 relative: the same seed refined by one quadratic Newton step
-// r(1 + e) (error e^2).  For the pivots of the factorization, whose scaled
-// columns and reciprocals carry that error into the solution at ~1e-12
-// relative (times the passive block's conditioning), below what the mixed
-// method's FP32 basis already moves it; one FP64 instruction fewer per pivot.
-__device__ __forceinline__ double pivot_rcp(double d) {
-    double r;
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
-    return fma(r, fma(-d, r, 1.0), r);
-}
 
 __device__ __forceinline__ double lane_pick(double v0, double v1, int i) {
     // value held for row i (rows i < 32 in v0, rows >= 32 in v1) broadcast from its lane
@@ -242,7 +232,7 @@ static __device__ __noinline__ bool gram_refactor(GramWS g, int k, double mu2) {
     for (int j = 0; j < k; ++j) {
         const double d = g.dd[j];
         if (!gt_nonneg_bits(d, lane_pick(th0, th1, j))) return false;  // d > tol * H_jj
-        const double rd = pivot_rcp(d);
+        const double rd = fast_rcp(d);
         const double yj = lane_pick(v0, v1, j);
         if (r0 > j && r0 < k) {
             const double c0 = L0[j], l0 = c0 * rd;
@@ -309,7 +299,7 @@ static __device__ __noinline__ bool gram_append(GramWS g, int k, int t, double m
     if (r1 < k) Lk[r1] = w1;
     if (lane == 0) {
         g.dd[k] = delta;
-        g.dinv[k] = pivot_rcp(delta);
+        g.dinv[k] = fast_rcp(delta);
         g.y[k] = yt;
         g.P[k] = t;
         g.pos[t] = k;
