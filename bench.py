@@ -362,6 +362,23 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def fp64_pipe_view(torch, ipv, Vp, kern_ms, clocks):
+    """The voxel kernel against the unit that binds it: FP64-pipe warp
+    instructions per second (ncu's count per voxel on a slab of the same
+    generator x voxels processed / kernel time) over the pipe's issue limit,
+    one warp instruction per 64 cycles per SM sub-partition (4 per SM) at the
+    SM clock sampled during the timed steps."""
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    if not mhz:
+        return None
+    achieved = ipv * Vp / (kern_ms * 1e-3) / 1e9
+    peak = 4 * sms * mhz * 1e6 / 64 / 1e9
+    return {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "G FP64 warp instructions/s",
+            "frac": achieved / peak, "instructions_per_voxel": ipv,
+            "peak_source": f"{sms} SMs x 4 sub-partitions x {mhz:.0f} MHz / 64 cycles per FP64 warp instruction"}
+
+
 def fp64_peak_tflops(torch):
     """cuBLAS DGEMM throughput on this GPU (the FP64 roofline denominator)."""
     n = 4096
@@ -821,6 +838,10 @@ def main():
                             f"operations (oracle-counted), which the mixed method replaces by fewer"}
     if "roofline" in line:
         line["roofline"]["hbm_view"] = hbm_view(mo, Vp, V, kern_ms)
+        method = "fp64" if args.precision == "fp64" else "mixed"
+        ipv = profile_figure(f"k_voxels_{method}_{args.workload}.md", "fp64_warp_instructions_per_voxel")
+        if ipv is not None:
+            line["roofline"]["fp64_pipe_view"] = fp64_pipe_view(torch, ipv, Vp, kern_ms, clk.summary())
     if args.workload == "lcurve48" and args.precision == "mixed" and not args.no_extra and world == 1:
         line["other_configurations"] = other_configurations(args, D, _lib, ctx, torch)
     print(json.dumps(line), flush=True)
