@@ -35,14 +35,23 @@ __device__ __forceinline__ double wsum(double v) {
 __device__ __forceinline__ double bcast(double v, int src) { return __shfl_sync(FULL, v, src); }
 __device__ __forceinline__ int bcasti(int v, int src) { return __shfl_sync(FULL, v, src); }
 
-// Julia's Base.max / Base.min for Float64 (NaN-propagating, -0.0 < 0.0).
+// Julia's Base.max / Base.min for Float64 (NaN-propagating, -0.0 < 0.0),
+// decided on the integer pipes: tkey orders non-NaN doubles as their values
+// with -0.0 below +0.0, which is the order signbit(x - y) gives (x - y is -0.0
+// only for x = -0.0, y = +0.0; for equal values, infinities included, x is
+// kept).
+__device__ __forceinline__ long long tkey(double d) {
+    const long long b = __double_as_longlong(d);
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool isnan_bits(double d);
 __device__ __forceinline__ double jmax(double x, double y) {
-    if (isnan(x) || isnan(y)) return CUDART_NAN;
-    return signbit(x - y) ? y : x;
+    if (isnan_bits(x) || isnan_bits(y)) return CUDART_NAN;
+    return tkey(x) < tkey(y) ? y : x;
 }
 __device__ __forceinline__ double jmin(double x, double y) {
-    if (isnan(x) || isnan(y)) return CUDART_NAN;
-    return signbit(x - y) ? x : y;
+    if (isnan_bits(x) || isnan_bits(y)) return CUDART_NAN;
+    return tkey(x) < tkey(y) ? x : y;
 }
 
 // Order-preserving integer image of a double for comparisons on the integer

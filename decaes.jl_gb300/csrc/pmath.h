@@ -50,10 +50,16 @@ PM_FN double pm_dbl_(uint64_t u) { double d; memcpy(&d, &u, 8); return d; }
 
 PM_FN double pm_pow2i(int k) { return PM_DBL((uint64_t)(k + 1023) << 52); }  // -1022 <= k <= 1023
 
+// The argument tests below compare bit patterns (integer operations, exact):
+// on the GPU they keep the FP64 pipe, the kernels' bottleneck, for arithmetic.
+#define PM_ABS_BITS 0x7fffffffffffffffULL
+#define PM_INF_BITS 0x7ff0000000000000ULL
+
 PM_FN double pm_exp(double x) {
-    if (x != x) return x;
-    if (x > 709.782712893384) return 1.0 / 0.0;
-    if (x < -745.1332191019412) return 0.0;
+    const uint64_t ub = PM_BITS(x);
+    if ((ub & PM_ABS_BITS) > PM_INF_BITS) return x;                           // NaN
+    if (!(ub >> 63) && ub > 0x40862e42fefa39efULL) return 1.0 / 0.0;         // x > 709.782712893384
+    if ((ub >> 63) && (ub & PM_ABS_BITS) > 0x40874910d52d3052ULL) return 0.0;  // x < -745.1332191019412
     double kd = rint(x * PM_INV_LN2);
     int k = (int)kd;
     double r = fma(-kd, PM_LN2_HI, x);
@@ -101,11 +107,11 @@ PM_FN double pm_expm1(double x) {
 }
 
 PM_FN double pm_log(double x) {
-    if (x != x) return x;
-    if (x < 0) return 0.0 / 0.0;
-    if (x == 0) return -1.0 / 0.0;
-    if (x == 1.0 / 0.0) return x;
     uint64_t u = PM_BITS(x);
+    if ((u & PM_ABS_BITS) > PM_INF_BITS) return x;  // NaN
+    if ((u & PM_ABS_BITS) == 0) return -1.0 / 0.0;  // +-0
+    if (u >> 63) return 0.0 / 0.0;                  // x < 0
+    if (u == PM_INF_BITS) return x;                 // +Inf
     int e = (int)((u >> 52) & 0x7ff);
     if (e == 0) {  // subnormal: scale by 2^54
         x = x * 18014398509481984.0;
@@ -114,7 +120,7 @@ PM_FN double pm_log(double x) {
     }
     e -= 1023;
     double f = PM_DBL((u & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL);
-    if (f > PM_SQRT2) {
+    if (PM_BITS(f) > 0x3ff6a09e667f3bcdULL) {  // f > sqrt(2), f in [1, 2)
         f = f * 0.5;
         e += 1;
     }

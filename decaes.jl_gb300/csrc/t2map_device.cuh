@@ -86,10 +86,17 @@ __device__ __forceinline__ long long ilkey(double d) {
     if ((b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) return 0x7fffffffffffffffLL;
     return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
 }
+// isapprox(x, y) with Julia's default rtol = sqrt(eps): x == y, or both
+// finite with |x - y| <= rtol * max(|x|, |y|).  Only the difference and the
+// tolerance are FP64 arithmetic; the tests and the max of two non-negative
+// finite values are bit-pattern comparisons (exact).
 __device__ __forceinline__ bool isapprox(double x, double y) {
-    if (x == y) return true;
-    if (!(isfinite(x) && isfinite(y))) return false;
-    return fabs(x - y) <= jmax(0.0, 1.4901161193847656e-08 * jmax(fabs(x), fabs(y)));
+    const long long bx = __double_as_longlong(x), by = __double_as_longlong(y);
+    const long long ax = bx & 0x7fffffffffffffffLL, ay = by & 0x7fffffffffffffffLL;
+    if ((bx == by && ax <= 0x7ff0000000000000LL) || (ax | ay) == 0) return true;  // x == y
+    if (ax >= 0x7ff0000000000000LL || ay >= 0x7ff0000000000000LL) return false;   // not both finite
+    const double tol = 1.4901161193847656e-08 * __longlong_as_double(ax < ay ? ay : ax);
+    return (__double_as_longlong(x - y) & 0x7fffffffffffffffLL) <= __double_as_longlong(tol);
 }
 // First i in [0, len) with isapprox(x, keys[i]), or -1; lanes over entries.
 static __device__ int warp_find_approx(const double *keys, int len, double x) {
