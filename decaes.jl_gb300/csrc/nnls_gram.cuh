@@ -201,8 +201,8 @@ static __device__ __noinline__ void gram_load(GramWS &g, const double *Gg, int n
 // with y = L^{-1} f_P carried along as an extra column.  Per pivot: one
 // reciprocal, the column scaled by the lanes of its rows, and the trailing
 // update -- diagonal included -- spread over lanes by (row, column) pair, so a
-// step costs ~(k-j)^2/64 FMA instructions instead of k-j.  Returns false when a pivot is not
-// positive relative to its diagonal (numerically dependent set).
+// step costs ~(k-j)^2/64 FMA instructions instead of k-j.  Returns false when
+// a pivot is not positive relative to its diagonal (numerically dependent set).
 static __device__ __noinline__ bool gram_refactor(GramWS g, int k, double mu2) {
     const int lane = threadIdx.x & 31;
     const int r0 = lane, r1 = lane + 32;
