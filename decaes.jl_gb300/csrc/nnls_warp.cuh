@@ -70,9 +70,11 @@ __device__ __forceinline__ bool pos_bits(double d) {
     const long long b = __double_as_longlong(d);
     return b > 0 && b <= 0x7ff0000000000000LL;
 }
-// d > t for a threshold t >= 0 or NaN, on the integer pipes: positive doubles
-// order like their bit patterns; negative d and NaN d give false, and so does
-// every d against a NaN threshold, as the FP64 comparison does.
+// d > t for a threshold t with its sign bit clear (+0.0 or positive) or NaN,
+// on the integer pipes: such doubles order like their bit patterns; negative d
+// and NaN d give false, and so does every d against a NaN threshold, as the
+// FP64 comparison does.  (t = -0.0 is not covered: +0.0 would compare above
+// it.  The solver's thresholds are tol * (sum of squares + mu^2), never -0.0.)
 __device__ __forceinline__ bool gt_nonneg_bits(double d, double t) {
     const long long b = __double_as_longlong(d);
     return b > __double_as_longlong(t) && b <= 0x7ff0000000000000LL && !isnan_bits(t);

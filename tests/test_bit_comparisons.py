@@ -1,7 +1,8 @@
 """The voxel kernels decide several FP64 comparisons on bit patterns (integer
 pipes) instead of the FP64 pipe: Julia's max/min (jmax/jmin,
-csrc/nnls_warp.cuh), isapprox with rtol = sqrt(eps) (csrc/t2map_device.cuh)
-and the argument tests of the portable exp/log (csrc/pmath.h).  This restates
+csrc/nnls_warp.cuh), isapprox with rtol = sqrt(eps) (csrc/t2map_device.cuh),
+the argument tests of the portable exp/log (csrc/pmath.h) and the solver's
+ordering, positivity and pivot tests (okey, pos_bits, gt_nonneg_bits).  This restates
 each bit-pattern rule in Python and checks it against the FP64 comparison it
 replaces, over special values (signed zeros, infinities, NaN, subnormals, the
 range limits) and random values at and around the tolerances.  The GPU's
@@ -172,3 +173,32 @@ def test_log_mantissa_split_matches_fp64():
     fs = [1.0 + k / 4096.0 for k in range(4096)] + [s2, math.nextafter(s2, 2.0), math.nextafter(s2, 0.0)]
     for f in fs:
         assert (f > s2) == (ubits(f) > 0x3FF6A09E667F3BCD), f
+
+
+# ---- the solver's earlier helpers (csrc/nnls_warp.cuh) -------------------------
+def okey(d):
+    b = bits(d)
+    if (b << 1) & 0xFFFFFFFFFFFFFFFF == 0:
+        return 0
+    return b if b >= 0 else b ^ M
+
+
+def pos_bits(d):
+    b = bits(d)
+    return 0 < b <= INF
+
+
+def gt_nonneg_bits(d, t):
+    b = bits(d)
+    return b > bits(t) and b <= INF and not isnan_bits(t)
+
+
+def test_solver_helpers_match_fp64(values):
+    finite_or_inf = [v for v in values if not math.isnan(v)]
+    for d in values:
+        assert pos_bits(d) == (d > 0), d
+    for a, c in itertools.product(finite_or_inf, repeat=2):
+        assert (okey(a) < okey(c)) == (a < c), (a, c)
+    thresholds = [t for t in values if math.isnan(t) or bits(t) >= 0]  # sign bit clear, as the solver's are
+    for d, t in itertools.product(values, thresholds):
+        assert gt_nonneg_bits(d, t) == (d > t), (d, t)
